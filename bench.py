@@ -1,0 +1,399 @@
+"""Benchmark: differentiated render + advect steps per second at 128^3 x 5 views.
+
+One step = MacCormack advection of the density by the MAC velocity, render of
+5 views (256x256 pixels, 128 depth samples, Beer-Lambert, BORDER), L2 loss to
+target images, and the backward to density and velocity -- the per-iteration
+work of the density / velocity reconstruction (configuration "differentiated
+single step").  Inputs are seeded synthetic plumes.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--dtype f32|bf16] [--impl ngt|reference]
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
+implementation of the same step (the NumPy restatement of the reference's
+operators; the reference itself has no CPU path and its CUDA build needs
+TensorFlow 1.12) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+bwd render+advect steps/s at 128^3 x 5 views"
+WORKLOAD = "MacCormack advect (MC_SMOOTH, CLAMP, dt=1) + 5-view Beer-Lambert raymarch 256x256x128 (BORDER) + L2 + backward to density and MAC velocity, 128^3 grid"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--dtype", default="f32", choices=["f32", "bf16", "f16"])
+    ap.add_argument("--impl", default="ngt", choices=["ngt", "reference"])
+    ap.add_argument("--grad-mode", default="exact", choices=["exact", "reference"])
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--cpu-baseline", default="on", choices=["on", "off"])
+    ap.add_argument("--kernel-stats", default="on", choices=["on", "off"])
+    return ap.parse_args()
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ngt" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value, device):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------- CPU legs
+def _cpu_adv_task(n):
+    """Advection forward + backward of the oracle on an n^3 grid."""
+    sys.path.insert(0, ROOT)
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from ngt_gb300 import synthetic
+    from oracle import advect
+    rho = synthetic.gaussian_blobs((n, n, n), seed=0)
+    ux, uy, uz = synthetic.curl_noise_mac((n, n, n), max_u=2.0, seed=1)
+    t0 = time.perf_counter()
+    out = advect.density_maccormack(rho, ux, uy, uz)
+    advect.density_maccormack_grad(rho, ux, uy, uz, out)
+    return time.perf_counter() - t0
+
+
+def _cpu_render_task(view, rows):
+    """Render forward + exact backward of ``rows`` image rows of one view, oracle."""
+    sys.path.insert(0, ROOT)
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from ngt_gb300 import workloads
+    from oracle import ops
+    w = workloads.config2()
+    D, H, W = w.image_dhw
+    # a band of rows through the image centre: same per-ray work as the full view
+    P = w.P[view:view + 1].copy()
+    Pm = P.reshape(4, 4).T.copy()
+    Pm[1, 1] *= H / rows  # narrow the frustum vertically to the band
+    P[0] = Pm.T.reshape(16)
+    F = w.F[view:view + 1].copy()
+    F[0, 4] *= rows / H
+    F[0, 5] *= rows / H
+    scale = np.asarray([w.depth_step, w.depth_step], np.float32)
+    x = (w.rho * scale).astype(np.float32)[None]
+    t0 = time.perf_counter()
+    y = ops.raymarch_grid_transform(x, w.M, w.V[view:view + 1], P, F, [D, rows, W])
+    g = np.zeros_like(y)
+    g[..., 0] = y[..., 0]
+    ops.raymarch_grid_transform_grad(x, y, g, w.M, w.V[view:view + 1], P, F, [D, rows, W])
+    return time.perf_counter() - t0
+
+
+def cpu_step_time(processes, adv_n=64, rows=8):
+    """Estimated seconds of one full step on the host: the advection timed on an
+    adv_n^3 grid and the render on ``rows`` rows of every view, each scaled
+    linearly by its share of the full work; with processes > 1 the render bands
+    run in parallel worker processes (spawned, no CUDA in them)."""
+    import multiprocessing as mp
+    full = 128 ** 3
+    t_adv = _cpu_adv_task(adv_n) * (full / adv_n ** 3)
+    views = 5
+    if processes > 1:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(min(processes, views)) as pool:
+            t0 = time.perf_counter()
+            pool.starmap(_cpu_render_task, [(v, rows) for v in range(views)])
+            t_render_wall = time.perf_counter() - t0
+        # rows of a view are independent: with P processes the full render takes
+        # (256/rows) * views bands / P band-times
+        per_band = t_render_wall / ((views + min(processes, views) - 1) // min(processes, views))
+        t_render = per_band * (256 / rows) * views / processes
+    else:
+        t_render = sum(_cpu_render_task(v, rows) for v in range(views)) * (256 / rows)
+    return t_adv + t_render, {"advect_sample": "%d^3 grid, scaled x%.0f" % (adv_n, full / adv_n ** 3),
+                              "render_sample": "%d of 256 rows per view, 5 views, scaled x%d" % (rows, 256 // rows)}
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        t, sample = cpu_step_time(procs, adv_n=48, rows=4)
+        if i >= args.warmup:
+            times.append(t)
+    value = 1.0 / float(np.mean(times))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": [128, 128, 128], "views": 5, "image": [256, 256],
+                       "depth_samples": 128},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": procs, "kind": "port",
+                             "sample": "NumPy restatement of the reference operators (the reference has no CPU "
+                                       "path); per step: %s; %s" % (sample["advect_sample"], sample["render_sample"])},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- GPU arm
+def gpu_arm(args, world, rank, local):
+    import torch
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from ngt_gb300 import _build, workloads
+    from ngt_gb300.step import RenderAdvectStep
+    _build.build_library()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workloads.config2()
+    st = {"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[args.dtype]
+
+    def dt(a):
+        return torch.as_tensor(a, device=dev).to(st).contiguous()
+
+    rho, ux, uy, uz = dt(w.rho), dt(w.ux), dt(w.uy), dt(w.uz)
+    # targets: render of the perturbed density (no advection)
+    from ngt_gb300 import ops
+    with torch.no_grad():
+        tgt = ops.raymarch_grid_transform(torch.as_tensor(w.rho_target, device=dev)[None], w.M, w.V, w.P, w.F,
+                                          w.image_dhw, emission_scale=(w.depth_step, w.depth_step))[..., :1]
+    step = RenderAdvectStep(rho, ux, uy, uz, w.M, w.V, w.P, w.F, tgt, w.image_dhw, grad_mode=args.grad_mode)
+    if not args.no_graph:
+        step.capture()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        step.step()
+    torch.cuda.synchronize()
+    # timed region: per-step device time between events; L2 flushed between steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step.step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    barrier(world)
+    clk = clocks.stop()
+    step_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
+    step_ms = max_over_ranks(world, step_ms, dev)
+    ms_per_step = step_ms / args.steps
+    value = world * 1e3 / ms_per_step  # whole job: every rank runs its own step (replicas)
+    loss_val = float(step.loss.item())
+
+    # per-call device times (no graph) for the roofline of the dominant kernel
+    kernel = None
+    if args.kernel_stats == "on":
+        kernel = kernel_stats(step, torch, dev, w, st, max(10, args.steps // 2), flush)
+
+    e2e = e2e_measure(torch, dev, w, st, tgt, args, flush)
+    samples = 2 * 2 * 128 ** 3 + 2 * 5 * 256 * 256 * 128
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.dtype,
+            "data": "synthetic (seeded Gaussian-blob density, curl-noise MAC velocity, 5 orbit cameras)",
+            "config": {"workload": WORKLOAD, "grid": [128, 128, 128], "views": 5, "image": [256, 256],
+                       "depth_samples": 128, "grad_mode": args.grad_mode, "cuda_graph": not args.no_graph,
+                       "l2": "flushed between timed steps (256 MiB write, outside the step events)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "voxel_samples_per_s": samples * value, "loss": loss_val,
+            "gpu_launches": RenderAdvectStep.KERNELS_PER_STEP * args.steps,
+            "wall_s_timed_region": t_wall,
+            "algorithmic_bytes_per_step": workloads.algorithmic_bytes((128, 128, 128), 5, (256, 256),
+                                                                      elem=torch.tensor([], dtype=st).element_size())}
+    peak, peak_kind = measured_peak_hbm()
+    line["hbm_frac_of_step"] = line["algorithmic_bytes_per_step"] / (ms_per_step * 1e-3) / (peak * 1e9)
+    if kernel:
+        name, avg_ms, nbytes = kernel
+        achieved = nbytes / (avg_ms * 1e-3) / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                            "algorithmic_bytes_per_launch": nbytes, "avg_ms": avg_ms}
+    if clk:
+        line["clocks"] = clk
+    line["e2e"] = e2e
+    if rank == 0 and world == 1 and args.cpu_baseline == "on":
+        t, sample = cpu_step_time(1, adv_n=48, rows=4)
+        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": 1, "kind": "port",
+                                "sample": "oracle (NumPy fp32, single process) per step: %s; %s"
+                                          % (sample["advect_sample"], sample["render_sample"])}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def kernel_stats(step, torch, dev, w, st, iters, flush):
+    """Average device time of each C-ABI call of the step (events around each
+    call, L2 flushed before each step) and the algorithmic bytes it moves."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    from ngt_gb300.ops import _ptr
+    es = torch.tensor([], dtype=st).element_size()
+    n_rho = 128 ** 3
+    n_u = 3 * 129 * 128 * 128
+    px = 5 * 256 * 256
+    nbytes = {
+        "advect_fwd": es * (2 * n_rho + n_u),                 # rho, u read; rho' written
+        "raymarch_fwd": es * n_rho + 4 * 2 * px,              # rho' read; image written
+        "image_l2_loss": 4 * (2 * px + px + 2 * px),          # image, target read; image grad written
+        "raymarch_bwd": es * n_rho + 4 * (2 * px * 2) + 4 * n_rho,  # rho', image, grad read; d rho' written
+        "advect_bwd": es * (n_rho + n_u) + 4 * (n_rho + n_rho) + 4 * (n_rho + n_u),  # rho,u,fwd,grad in; grads out
+    }
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    calls = [("advect_fwd", lambda: step._call("ngt_advect_maccormack_fwd", ctypes.byref(step.adv), s)),
+             ("raymarch_fwd", lambda: step._call("ngt_raymarch_fwd", ctypes.byref(step.ray), s)),
+             ("image_l2_loss", lambda: step._call("ngt_image_l2_loss", L.F32, step.pixels, 2, 1, _ptr(step.image),
+                                                  _ptr(step.targets), _ptr(step.g_image), _ptr(step.loss), s)),
+             ("raymarch_bwd", lambda: step._call("ngt_raymarch_bwd", ctypes.byref(step.ray_g), s)),
+             ("advect_bwd", lambda: step._call("ngt_advect_maccormack_bwd", ctypes.byref(step.adv_g), s))]
+    tot = {n: 0.0 for n, _ in calls}
+    for it in range(iters + 2):
+        flush.zero_()
+        evs = []
+        for n, fn in calls:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            evs.append((n, a, b))
+        torch.cuda.synchronize()
+        if it >= 2:
+            for n, a, b in evs:
+                tot[n] += a.elapsed_time(b)
+    name = max(tot, key=tot.get)
+    return name, tot[name] / iters, nbytes[name]
+
+
+def e2e_measure(torch, dev, w, st, tgt, args, flush):
+    """Same step through the public autograd API, with the density and velocity
+    copied from pinned host memory every step and the loss read back."""
+    from ngt_gb300 import advect, ops
+    host = [torch.as_tensor(a).to(st).pin_memory() for a in (w.rho, w.ux, w.uy, w.uz)]
+    h2d = sum(t.numel() * t.element_size() for t in host)
+    scale = (w.depth_step, w.depth_step)
+
+    def one():
+        ts = [t.to(dev, non_blocking=True).requires_grad_() for t in host]
+        r2 = advect.warp(ts[0], ts[1], ts[2], ts[3], dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP")
+        img = ops.raymarch_grid_transform(r2[None], w.M, w.V, w.P, w.F, w.image_dhw, emission_scale=scale)
+        loss = 0.5 * ((img[..., :1] - tgt) ** 2).sum()
+        loss.backward()
+        return float(loss.item())
+
+    for _ in range(max(2, args.warmup)):
+        one()
+    torch.cuda.synchronize()
+    n = max(5, args.steps // 2)
+    tot = 0.0
+    for _ in range(n):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        one()
+        tot += time.perf_counter() - t0
+    return {"value": n / tot, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
+            "path": "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + torch loss.backward()"}
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        gpu_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

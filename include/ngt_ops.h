@@ -1,0 +1,291 @@
+/*
+ * ngt_ops.h -- C ABI of the GB300 (sm_103a) differentiable grid operators.
+ *
+ * Drop-in boundary for the operator layer of Neural-Global-Transport's
+ * reconstruction loop (phitest/render/cuda).  Each forward / backward pair
+ * replaces one TensorFlow custom op and the gradient registered for it in
+ * phitest/render/cuda/ops_loader.py; attribute names and meanings are kept
+ * (enums below), shapes follow the ops' NDHWC conventions.
+ *
+ * Conventions
+ *  - All data pointers are device pointers; the library allocates nothing.
+ *    Outputs, gradients and any workspace are owned by the caller.  Every
+ *    op that needs scratch memory reports its size through the matching
+ *    *_workspace_bytes() query.
+ *  - Matrices (model M per batch entry, view V / projection P per camera)
+ *    are 16 floats read column-major, exactly the buffer the reference ops
+ *    receive (renderer.py:117-121 passes matrix.transpose()); frusta are 6
+ *    floats [near, far, left, right, top, bottom] (camera.py:64-65).  They
+ *    are read on the device, so a call can be captured in a CUDA graph.
+ *  - ``stream`` is a cudaStream_t passed as void*; all work is ordered on it
+ *    and no call synchronises the host.
+ *  - Return value: NGT_OK or an NGT_ERR_* code; ngt_last_error_message()
+ *    describes the last failure of the calling thread.  No call exits or
+ *    traps (the reference calls exit(10) on CUDA errors,
+ *    kernel_setup.hpp:44-50).
+ *  - Gradients come in two semantics: NGT_GRAD_EXACT is the true adjoint of
+ *    the forward; NGT_GRAD_REFERENCE reproduces the reference's registered
+ *    gradients (per-voxel division by sample counts / summed sample weights,
+ *    resample_grid.cu.cc:1133-1151, raymarch_grid.cu.cc:458-480, and the
+ *    raymarch backward's own sampling positions, raymarch_grid.cu.cc:508-518).
+ */
+#ifndef NGT_OPS_H
+#define NGT_OPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define NGT_OK 0
+#define NGT_ERR_INVALID_ARGUMENT 1 /* shape, channel count, enum or pointer rejected */
+#define NGT_ERR_UNSUPPORTED 2      /* valid but unsupported combination */
+#define NGT_ERR_CUDA 3             /* a CUDA launch or copy failed */
+#define NGT_ERR_WORKSPACE 4        /* workspace missing or too small */
+
+/* ------------------------------------------------------------------ enums */
+/* storage type of grids / images; arithmetic is float32 (float64 for F64) */
+enum { NGT_F32 = 0, NGT_F64 = 1, NGT_BF16 = 2, NGT_F16 = 3 };
+/* attr interpolation (resample_grid.cc:32,100; raymarch_grid.cc:37) */
+enum { NGT_NEAREST = 0, NGT_LINEAR = 1, NGT_MIN = 2, NGT_MAX = 3, NGT_QUADRATIC = 4 };
+/* attr boundary (resample_grid.cc:33,101; raymarch_grid.cc:38) */
+enum { NGT_BORDER = 0, NGT_CLAMP = 1, NGT_WRAP = 2 };
+/* attr mipmapping (resample_grid.cc:34) */
+enum { NGT_MIP_NONE = 0, NGT_MIP_NEAREST = 1, NGT_MIP_LINEAR = 2 };
+/* attr blending_mode (raymarch_grid.cc:44, reduce_blend.cc:26) */
+enum { NGT_BEER_LAMBERT = 0, NGT_ALPHA = 2, NGT_ALPHA_ADDITIVE = 3, NGT_ADDITIVE = 4 };
+/* attr coordinate_mode (resample_grid.cc:40) */
+enum { NGT_TRANSFORM_LINDEPTH = 0, NGT_TRANSFORM_LINDEPTH_REVERSE = 1, NGT_TRANSFORM = 3,
+       NGT_TRANSFORM_REVERSE = 4 };
+/* gradient semantics */
+enum { NGT_GRAD_EXACT = 0, NGT_GRAD_REFERENCE = 1 };
+/* advection clamp (data_structures.py:1715-1735) */
+enum { NGT_CLAMP_NONE = 0, NGT_CLAMP_MC_SMOOTH = 1, NGT_CLAMP_NEGATIVE = 2 };
+
+/* ------------------------------------------------------------ LUT resample */
+/* Replaces op SampleGridLut (resample_grid.cc:94-120, 742-899) and its
+ * gradient op SampleGridLutGrad (resample_grid.cc:124-150, 925-1081) as
+ * registered in ops_loader.py:41-60. */
+typedef struct {
+  int32_t dtype;              /* NGT_F32 or NGT_F64 (lookup uses the same type) */
+  int64_t input_shape[5];     /* N, D, H, W, C with C in {1, 2, 4} */
+  int64_t lookup_shape[5];    /* V, D', H', W', 4 (x, y, z, LoD) */
+  const void* input;          /* NDHWC */
+  const void* lookup;         /* V D' H' W' 4 */
+  void* output;               /* N, V (1 unless separate_camera_batch), D', H', W', C */
+  int32_t interpolation;      /* NEAREST, LINEAR, MIN, MAX */
+  int32_t boundary;           /* BORDER, CLAMP, WRAP */
+  int32_t mipmapping;         /* NONE, NEAREST, LINEAR */
+  int32_t num_mipmaps;
+  float mip_bias;
+  float cell_center_offset;   /* default 0.0; must be 0.5 with normalized coordinates */
+  int32_t separate_camera_batch;
+  int32_t relative_coords;
+  int32_t normalized_coords;
+  void* workspace;            /* mip pyramid when mipmapping != NONE */
+  size_t workspace_bytes;
+} ngt_sample_lut_args;
+
+typedef struct {
+  ngt_sample_lut_args fwd;    /* the forward call's arguments (fwd.output unused) */
+  const void* output_grad;    /* shape of fwd.output */
+  void* input_grad;           /* shape of fwd.input */
+  void* lookup_grad;          /* shape of fwd.lookup; may be null */
+  int32_t grad_mode;          /* NGT_GRAD_EXACT / NGT_GRAD_REFERENCE */
+  void* workspace;            /* per-voxel sample counts (reference mode) */
+  size_t workspace_bytes;
+} ngt_sample_lut_grad_args;
+
+int ngt_sample_lut_fwd(const ngt_sample_lut_args* args, void* stream);
+size_t ngt_sample_lut_fwd_workspace_bytes(const ngt_sample_lut_args* args);
+int ngt_sample_lut_bwd(const ngt_sample_lut_grad_args* args, void* stream);
+size_t ngt_sample_lut_bwd_workspace_bytes(const ngt_sample_lut_grad_args* args);
+
+/* ------------------------------------------------------ transform resample */
+/* Replaces op SampleGridTransform (resample_grid.cc:23-65, 316-516) and
+ * SampleGridTransformGrad (resample_grid.cc:68-92, 538-717) as registered in
+ * ops_loader.py:19-39. */
+typedef struct {
+  int32_t dtype;              /* NGT_F32 or NGT_F64 */
+  int64_t input_shape[5];     /* N, D, H, W, C with C in {1, 2, 4} */
+  int64_t output_dhw[3];      /* D', H', W' of the sampled grid */
+  const void* input;
+  const float* matrix_m;      /* N x 16 */
+  const float* matrix_v;      /* V x 16 */
+  const float* matrix_p;      /* V x 16 */
+  const float* frustum;       /* V x 6 */
+  int32_t num_cameras;        /* V */
+  void* output;               /* N, V (1 unless separate_camera_batch), D', H', W', C */
+  int32_t interpolation;      /* NEAREST, LINEAR, QUADRATIC */
+  int32_t boundary;           /* BORDER, CLAMP */
+  int32_t mipmapping;
+  int32_t num_mipmaps;
+  float mip_bias;
+  float cell_center_offset;   /* default 0.5 */
+  int32_t coordinate_mode;
+  int32_t separate_camera_batch;
+  void* workspace;            /* mip pyramid when mipmapping != NONE */
+  size_t workspace_bytes;
+} ngt_sample_transform_args;
+
+typedef struct {
+  ngt_sample_transform_args fwd;
+  const void* output_grad;
+  void* input_grad;
+  int32_t grad_mode;
+  void* workspace;            /* per-voxel sample counts (reference mode) */
+  size_t workspace_bytes;
+} ngt_sample_transform_grad_args;
+
+int ngt_sample_transform_fwd(const ngt_sample_transform_args* args, void* stream);
+size_t ngt_sample_transform_fwd_workspace_bytes(const ngt_sample_transform_args* args);
+int ngt_sample_transform_bwd(const ngt_sample_transform_grad_args* args, void* stream);
+size_t ngt_sample_transform_bwd_workspace_bytes(const ngt_sample_transform_grad_args* args);
+
+/* Mip pyramid of a grid (MipAtlas3D, resample_grid.cu.cc:116-251): levels 1..L
+ * written back to back into ``pyramid`` (each level (D>>l, H>>l, W>>l, C)). */
+int ngt_mip_build(int32_t dtype, const int64_t input_shape[5], const void* input, int32_t levels, void* pyramid,
+                  size_t pyramid_bytes, void* stream);
+size_t ngt_mip_bytes(int32_t dtype, const int64_t input_shape[5], int32_t levels);
+
+/* Replaces op LodTransform (resample_grid.cc:152-172, 1089-1178): per camera a
+ * lookup table (x, y, z, LoD) of the sampling positions of a transform resample. */
+typedef struct {
+  int64_t input_dhw[3];       /* grid sampled from */
+  int64_t output_dhw[3];      /* grid sampled to */
+  const float* matrix_mv;     /* V x 16 model-view */
+  const float* matrix_p;      /* V x 16 */
+  const float* frustum;       /* V x 6 */
+  int32_t num_cameras;
+  int32_t inverse_transform;
+  int32_t linearize_depth;
+  int32_t relative_coords;
+  float* output;              /* V, D', H', W', 4 (float32) */
+} ngt_lod_args;
+int ngt_lod_transform(const ngt_lod_args* args, void* stream);
+
+/* ------------------------------------------------------------ fused raymarch */
+/* Replaces op RaymarchGridTransform (raymarch_grid.cc:29-63, 186-320) and
+ * RaymarchGridTransformGrad (raymarch_grid.cc:67-92, 342-504) as registered in
+ * ops_loader.py:73-95. */
+typedef struct {
+  int32_t dtype;              /* NGT_F32, NGT_F64, NGT_BF16, NGT_F16 (storage of input) */
+  int64_t input_shape[5];     /* N, D, H, W, C with C in {1, 2, 4} */
+  int64_t output_dhw[3];      /* depth samples D', image H', W' */
+  const void* input;
+  const float* matrix_m;      /* N x 16 */
+  const float* matrix_v;      /* V x 16 */
+  const float* matrix_p;      /* V x 16 */
+  const float* frustum;       /* V x 6 */
+  int32_t num_cameras;
+  void* output;               /* N, V (1 unless separate_camera_batch), H', W', Cb (float32/64) */
+  int32_t interpolation;      /* NEAREST, LINEAR, MIN, MAX (gradient: LINEAR) */
+  int32_t boundary;
+  int32_t blending_mode;
+  int32_t keep_dims;          /* output N, V, 1, H', W', Cb */
+  int32_t separate_camera_batch;
+  /* Emission expansion: with emission_channels = Cb > 0 the input has one
+   * channel (density) and the blend sees Cb channels, channel c being
+   * emission_scale[c] * sample.  This is the renderer's light grid
+   * [rho*c*i*step, rho*step] (lighting.py:26-34, renderer.py:533-548,763)
+   * formed on the fly instead of materialised. 0 = off (Cb = C). */
+  int32_t emission_channels;
+  float emission_scale[4];
+} ngt_raymarch_args;
+
+typedef struct {
+  ngt_raymarch_args fwd;
+  const void* output;         /* the forward's output */
+  const void* output_grad;    /* same shape */
+  void* input_grad;           /* shape of fwd.input (float32/64) */
+  int32_t grad_mode;
+  void* workspace;            /* sample-weight sums (reference mode) */
+  size_t workspace_bytes;
+} ngt_raymarch_grad_args;
+
+int ngt_raymarch_fwd(const ngt_raymarch_args* args, void* stream);
+int ngt_raymarch_bwd(const ngt_raymarch_grad_args* args, void* stream);
+size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* args);
+
+/* ------------------------------------------------------------ reduce blend */
+/* Replaces op ReduceGridBlend / ReduceGridBlendGrad (reduce_blend.cc:24-56,
+ * 68-252) as registered in ops_loader.py:64-69. */
+typedef struct {
+  int32_t dtype;              /* NGT_F32 or NGT_F64 */
+  int64_t input_shape[5];     /* N, D, H, W, C */
+  const void* input;
+  void* output;               /* N, H, W, C or N, D, H, W, C with keep_dims */
+  int32_t blending_mode;
+  int32_t keep_dims;
+} ngt_reduce_blend_args;
+
+typedef struct {
+  ngt_reduce_blend_args fwd;
+  const void* output;
+  const void* output_grad;
+  void* input_grad;
+  int32_t grad_mode;
+} ngt_reduce_blend_grad_args;
+
+int ngt_reduce_blend_fwd(const ngt_reduce_blend_args* args, void* stream);
+int ngt_reduce_blend_bwd(const ngt_reduce_blend_grad_args* args, void* stream);
+
+/* ------------------------------------------------------ MacCormack advection */
+/* Fused semi-Lagrangian / MacCormack warp of a cell-centred grid by a
+ * MAC-staggered velocity.  Replaces the TensorFlow composition of
+ * VelocityGrid.warp (data_structures.py:1690-1737: centred velocity, LUT
+ * sample forward, LUT sample back, correction, MIN / MAX lookups, revert
+ * clamp) -- four SampleGridLut calls and their registered gradients. */
+typedef struct {
+  int32_t dtype;              /* NGT_F32, NGT_F64, NGT_BF16, NGT_F16 (storage) */
+  int64_t grid_dhw[3];        /* D, H, W of the advected grid */
+  int32_t channels;           /* C in {1, 2, 4} */
+  const void* data;           /* D, H, W, C */
+  const void* vel_x;          /* D, H, W+1 */
+  const void* vel_y;          /* D, H+1, W */
+  const void* vel_z;          /* D+1, H, W */
+  float dt;
+  int32_t order;              /* 1 semi-Lagrangian, 2 MacCormack */
+  int32_t clamp;              /* NGT_CLAMP_* */
+  int32_t boundary;           /* BORDER, CLAMP, WRAP (configs: CLAMP) */
+  void* output;               /* D, H, W, C */
+  void* fwd_field;            /* D, H, W, C scratch written by the forward (order 2), read by the backward */
+} ngt_advect_args;
+
+typedef struct {
+  ngt_advect_args fwd;        /* fwd.output unused; fwd.fwd_field as written by the forward */
+  const void* output_grad;
+  void* data_grad;            /* D, H, W, C */
+  void* vel_x_grad;           /* face grids, may all be null */
+  void* vel_y_grad;
+  void* vel_z_grad;
+  int32_t grad_mode;
+  void* workspace;
+  size_t workspace_bytes;
+} ngt_advect_grad_args;
+
+int ngt_advect_maccormack_fwd(const ngt_advect_args* args, void* stream);
+int ngt_advect_maccormack_bwd(const ngt_advect_grad_args* args, void* stream);
+size_t ngt_advect_maccormack_bwd_workspace_bytes(const ngt_advect_grad_args* args);
+
+/* ------------------------------------------------------------ step helpers */
+/* Image loss of the reconstruction step, 0.5 * sum over pixels of
+ * (image[..., c] - target[..., c])^2 for the first ``loss_channels`` channels
+ * (loss_dens_target, optimization.py:478, on the rendered light channel).
+ * Writes the image gradient (zero in the remaining channels) and adds the loss
+ * to *loss (device float; zero it first).  No reference counterpart as a
+ * single call: the reference forms this loss with TensorFlow ops. */
+int ngt_image_l2_loss(int32_t dtype, int64_t pixels, int32_t channels, int32_t loss_channels, const void* image,
+                      const void* target, void* image_grad, float* loss, void* stream);
+
+/* ------------------------------------------------------------ diagnostics */
+const char* ngt_last_error_message(void);
+int ngt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NGT_OPS_H */

@@ -1,0 +1,117 @@
+"""Semi-Lagrangian / MacCormack advection by a MAC-staggered velocity.
+
+``warp`` is the fused replacement of ``VelocityGrid.warp``
+(phitest/render/data_structures.py:1690-1737) -- which the reference composes
+from four ``SampleGridLut`` calls and TensorFlow elementwise ops -- and is
+differentiable w.r.t. the advected grid and all three face grids.
+"""
+import ctypes
+
+import torch
+
+from . import _lib as L
+from .ops import _code, _cuda, _ptr, _stream, _workspace, compute_dtype, get_gradient_mode
+
+
+def _spatial(t, name):
+    """Accept (D,H,W,C), (1,D,H,W,C), (D,H,W) or (1,D,H,W,1) layouts."""
+    t = _cuda(t, name)
+    if t.dim() == 5:
+        if t.shape[0] != 1:
+            raise ValueError("%s: batch must be 1" % name)
+        t = t[0]
+    return t.contiguous()
+
+
+def _faces(t, name):
+    t = _spatial(t, name)
+    if t.dim() == 4:
+        if t.shape[-1] != 1:
+            raise ValueError("%s: a face grid has one channel" % name)
+        t = t[..., 0]
+    return t.contiguous()
+
+
+def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary):
+    a = L.AdvectArgs()
+    a.dtype = _code(data)
+    D, H, W, C = data.shape
+    a.grid_dhw = L.I64x3(D, H, W)
+    a.channels = C
+    a.data, a.vel_x, a.vel_y, a.vel_z = _ptr(data), _ptr(vx), _ptr(vy), _ptr(vz)
+    a.dt = float(dt)
+    a.order = int(order)
+    a.clamp = L.CLAMP[clamp.upper()]
+    a.boundary = L.BOUNDARY[boundary]
+    a.output, a.fwd_field = _ptr(out), _ptr(fwd)
+    return a
+
+
+def _check_faces(data, vx, vy, vz):
+    D, H, W = data.shape[:3]
+    if tuple(vx.shape) != (D, H, W + 1) or tuple(vy.shape) != (D, H + 1, W) or tuple(vz.shape) != (D + 1, H, W):
+        raise ValueError("shapes of components do not fit: data %s, x %s, y %s, z %s"
+                         % (tuple(data.shape), tuple(vx.shape), tuple(vy.shape), tuple(vz.shape)))
+
+
+def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP"):
+    """Forward only; returns (output, fwd_field) with fwd_field kept for the backward."""
+    out = torch.empty_like(data)
+    fwd = torch.empty(data.shape, dtype=compute_dtype(data), device=data.device) if order == 2 else None
+    L.call("ngt_advect_maccormack_fwd", ctypes.byref(_args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary)),
+           _stream())
+    return out, fwd
+
+
+def warp_backward(data, vx, vy, vz, fwd, grad, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP",
+                  grad_mode=None, velocity_grad=True):
+    cd = compute_dtype(data)
+    g = L.AdvectGradArgs()
+    g.fwd = _args(data, vx, vy, vz, None, fwd, dt, order, clamp, boundary)
+    gd = torch.empty(data.shape, dtype=cd, device=data.device)
+    gx = torch.empty(vx.shape, dtype=cd, device=data.device) if velocity_grad else None
+    gy = torch.empty(vy.shape, dtype=cd, device=data.device) if velocity_grad else None
+    gz = torch.empty(vz.shape, dtype=cd, device=data.device) if velocity_grad else None
+    g.output_grad, g.data_grad = _ptr(grad.to(cd).contiguous()), _ptr(gd)
+    g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = _ptr(gx), _ptr(gy), _ptr(gz)
+    g.grad_mode = L.GRAD[grad_mode or get_gradient_mode()]
+    ws = _workspace(L.load().ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g)), data.device)
+    g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
+    keep = grad.to(cd).contiguous()
+    g.output_grad = _ptr(keep)
+    L.call("ngt_advect_maccormack_bwd", ctypes.byref(g), _stream())
+    return gd, gx, gy, gz
+
+
+class _Warp(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, data, vx, vy, vz, dt, order, clamp, boundary):
+        out, fwd = warp_forward(data, vx, vy, vz, dt, order, clamp, boundary)
+        ctx.save_for_backward(data, vx, vy, vz, fwd)
+        ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode())
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        data, vx, vy, vz, fwd = ctx.saved_tensors
+        dt, order, clamp, boundary, mode = ctx.cfg
+        gd, gx, gy, gz = warp_backward(data, vx, vy, vz, fwd, grad.contiguous(), dt, order, clamp, boundary, mode,
+                                       velocity_grad=any(ctx.needs_input_grad[1:4]))
+        return gd, gx, gy, gz, None, None, None, None
+
+
+def warp(data, vel_x, vel_y, vel_z, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP"):
+    """Advect ``data`` (D,H,W,C) -- or (1,D,H,W,C) -- by the MAC velocity
+    (x: D,H,W+1; y: D,H+1,W; z: D+1,H,W).  order 1 is semi-Lagrangian, order 2
+    MacCormack; clamp 'MC_SMOOTH' reverts to the semi-Lagrangian value where the
+    correction leaves the range of the forward lookup's corners, 'NEGATIVE'
+    clips at 0, 'NONE' does neither."""
+    lead = data.dim() == 5
+    d = _spatial(data, "data")
+    vx, vy, vz = _faces(vel_x, "vel_x"), _faces(vel_y, "vel_y"), _faces(vel_z, "vel_z")
+    _check_faces(d, vx, vy, vz)
+    if clamp.upper() == "MC":
+        raise NotImplementedError("MIM and MAX warp sampling have wrong gradients.")
+    out = _Warp.apply(d, vx.to(d.dtype), vy.to(d.dtype), vz.to(d.dtype), float(dt), int(order), clamp.upper(),
+                      boundary)
+    return out[None] if lead else out

@@ -1,0 +1,589 @@
+// Fused frustum raymarch: per-pixel ray through the volume, sample + blend
+// front to back (forward), and its gradients.
+//
+// Semantics follow the reference kernels kRaymarchGridTransformLindepth
+// (raymarch_grid.cu.cc:202-252) and kRaymarchGridTransformLindepthGrad
+// (:482-521): rays run from frustum-grid index z = 0.5 to z = max(D'-1,1)+0.5 in
+// object space (getRaymarchStep, :173-200); with BORDER they are clipped to the
+// box through the outer cell centres (RayGridIntersectionDistances, :109-165)
+// with one step of margin; sample positions accumulate ``pos += step``.
+//
+// GB300 layout: one thread per ray, a 16x8-pixel tile per 128-thread block
+// (each warp an 8x4 sub-tile, so the 32 rays of a warp gather from nearby
+// cells and hit L1); blockIdx.y enumerates (batch, camera) slots and the
+// block's camera matrices are formed once in shared memory.
+#include "ngt_common.cuh"
+#include "ngt_host.cuh"
+#include "ngt_blend.cuh"
+
+namespace ngt {
+namespace {
+
+constexpr int kTileX = 16, kTileY = 8, kThreads = kTileX * kTileY;
+constexpr int kSeg = 16;       // exact backward: steps recomputed per segment buffer
+constexpr int kMaxCkpt = 64;   // exact backward: checkpoints per ray
+constexpr int kMaxSteps = 1 << 20;
+
+struct RayParams {
+  const void* input;
+  void* output;
+  const void* out_fwd;   // backward: forward output
+  const void* out_grad;  // backward: output gradient
+  void* in_grad;         // backward: input gradient (compute type)
+  void* wbuf;            // reference backward: weighted gradient buffer
+  void* wsum;            // reference backward: per-voxel weight sums
+  const float *M, *V, *P, *F;
+  Dims din;
+  int D, H, W;           // depth samples, image height, width
+  int N, ncam, sep;
+  int fm, bm, blend;
+  float scale[4];
+  int slot0;             // first (batch, camera) slot of this launch
+};
+
+__device__ __forceinline__ void slot_to_bc(const RayParams& p, int slot, int& b, int& c, int& oslot) {
+  if (p.sep) {
+    b = slot / p.ncam;
+    c = slot % p.ncam;
+  } else {
+    b = slot;
+    c = slot;
+  }
+  oslot = slot;
+}
+
+__device__ __forceinline__ void pixel_of_thread(int& px, int& py) {
+  const int t = threadIdx.x;
+  const int lane = t & 31, warp = t >> 5;
+  const int tiles_x = 0;  // unused
+  (void)tiles_x;
+  px = (warp & 1) * 8 + (lane & 7);
+  py = (warp >> 1) * 4 + (lane >> 3);
+}
+
+struct Ray {
+  float s[3], st[3], e[3];
+  int steps;
+  bool hit;
+};
+
+// getRaymarchStep / RayGridIntersectionDistances (raymarch_grid.cu.cc:109-200)
+__device__ inline Ray ray_setup(const Cam& cam, int px, int py, const RayParams& p) {
+  Ray r;
+  const float dinv[3] = {1.0f / float(p.W), 1.0f / float(p.H), 1.0f / float(p.D)};
+  const float zmax = float(max(p.D - 1, 1));
+  idx_to_os(cam, px + 0.5f, py + 0.5f, 0.5f, dinv, false, r.s);
+  idx_to_os(cam, px + 0.5f, py + 0.5f, zmax + 0.5f, dinv, false, r.e);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) r.st[a] = (r.e[a] - r.s[a]) / zmax;
+  r.steps = p.D;
+  r.hit = true;
+  if (p.bm == BORDER) {
+    float v[3] = {r.e[0] - r.s[0], r.e[1] - r.s[1], r.e[2] - r.s[2]};
+    const float il = rsqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const float dir[3] = {v[0] * il, v[1] * il, v[2] * il};
+    const float bmax[3] = {float(p.din.x), float(p.din.y), float(p.din.z)};
+    float tmin = -INFINITY, tmax = INFINITY;
+    float tsm[3], tbg[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float half = bmax[a] * 0.5f + (-0.5f);
+      const float co = r.s[a] - bmax[a] * 0.5f;
+      const float inv = 1.0f / dir[a];
+      const float n = inv * co;
+      const float k = fabsf(inv) * half;
+      tsm[a] = 0.0f - n - k;
+      tbg[a] = k - n;
+    }
+    tmin = fmaxf(fmaxf(tsm[0], tsm[1]), tsm[2]);
+    tmax = fminf(fminf(tbg[0], tbg[1]), tbg[2]);
+    if (tmin > tmax || tmax < 0.0f) {
+      r.hit = false;
+      r.steps = 0;
+      return r;
+    }
+    float e2[3], s2[3];
+    const float t0 = fmaxf(tmin - 1.0f, 0.0f);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      e2[a] = r.s[a] + dir[a] * (tmax + 1.0f);
+      s2[a] = r.s[a] + dir[a] * t0;
+    }
+    const float ss = sqrtf(r.st[0] * r.st[0] + r.st[1] * r.st[1] + r.st[2] * r.st[2]);
+    const float d0 = s2[0] - e2[0], d1 = s2[1] - e2[1], d2 = s2[2] - e2[2];
+    const float rl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+    const float q = rl / ss;
+    r.steps = (q < float(kMaxSteps)) ? int(q) + 2 : kMaxSteps;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      r.s[a] = s2[a];
+      r.e[a] = e2[a];
+    }
+  }
+  return r;
+}
+
+// Sample CIN channels at object-space position pos and expand to CB blend channels.
+template <int CIN, int CB, class T, class S>
+__device__ __forceinline__ void sample_cell(const T* __restrict__ g, const float pos[3], const RayParams& p,
+                                            S cell[CB]) {
+  const S px = S(pos[0] - 0.5f), py = S(pos[1] - 0.5f), pz = S(pos[2] - 0.5f);
+  S v[CIN];
+  if (p.fm == LINEAR) {
+    read_linear<CIN>(g, px, py, pz, p.din, p.bm, v);
+  } else if (p.fm == NEAREST) {
+    read_nearest<CIN>(g, px, py, pz, p.din, p.bm, v);
+  } else {
+    int arg[CIN];
+    int64_t ci[8];
+    read_extremum<CIN>(g, px, py, pz, p.din, p.bm, p.fm == FMAX, v, arg, ci);
+  }
+  if (CIN == CB) {
+#pragma unroll
+    for (int c = 0; c < CB; ++c) cell[c] = v[c < CIN ? c : 0];
+  } else {
+#pragma unroll
+    for (int c = 0; c < CB; ++c) cell[c] = S(p.scale[c]) * v[0];
+  }
+}
+
+template <int CIN, int CB, class S>
+__device__ __forceinline__ void scatter_cell(const RayParams& p, S* __restrict__ grad, const float pos[3],
+                                             const S dcell[CB]) {
+  const S px = S(pos[0] - 0.5f), py = S(pos[1] - 0.5f), pz = S(pos[2] - 0.5f);
+  if (CIN == CB) {
+    S g[CIN];
+#pragma unroll
+    for (int c = 0; c < CIN; ++c) g[c] = dcell[c < CB ? c : 0];
+    scatter_linear<CIN>(grad, px, py, pz, p.din, p.bm, g);
+  } else {
+    S g[1] = {S(0)};
+#pragma unroll
+    for (int c = 0; c < CB; ++c) g[0] += S(p.scale[c]) * dcell[c];
+    scatter_linear<1>(grad, px, py, pz, p.din, p.bm, g);
+  }
+}
+
+__device__ __forceinline__ void load_cam(const RayParams& p, int b, int c, Cam& cam) {
+  build_cam(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam);
+}
+
+// ----------------------------------------------------------------- forward
+template <int CIN, int CB, class T, class S>
+__global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
+  __shared__ Cam cam;
+  int b, c, oslot;
+  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
+  if (threadIdx.x == 0) load_cam(p, b, c, cam);
+  __syncthreads();
+  const int tiles_x = (p.W + kTileX - 1) / kTileX;
+  int px, py;
+  pixel_of_thread(px, py);
+  px += (blockIdx.x % tiles_x) * kTileX;
+  py += (blockIdx.x / tiles_x) * kTileY;
+  if (px >= p.W || py >= p.H) return;
+  const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  const Ray r = ray_setup(cam, px, py, p);
+  S acc[CB];
+#pragma unroll
+  for (int k = 0; k < CB; ++k) acc[k] = S(0);
+  if (r.hit) {
+    float pos[3] = {r.s[0], r.s[1], r.s[2]};
+    for (int i = 0; i < r.steps; ++i) {
+      S cell[CB];
+      sample_cell<CIN, CB>(g, pos, p, cell);
+      blend_step<CB>(acc, cell, p.blend);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
+    }
+  }
+  S* out = reinterpret_cast<S*>(p.output) + ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
+#pragma unroll
+  for (int k = 0; k < CB; ++k) out[k] = acc[k];
+}
+
+// ------------------------------------------------------- exact backward
+// Accumulator states are recomputed forward (checkpoints every K steps, then
+// each segment re-marched into a small buffer and walked back), so the adjoint
+// uses the forward's own positions and densities, not a subtraction.
+template <int CIN, int CB, class T, class S>
+__global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
+  __shared__ Cam cam;
+  int b, c, oslot;
+  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
+  if (threadIdx.x == 0) load_cam(p, b, c, cam);
+  __syncthreads();
+  const int tiles_x = (p.W + kTileX - 1) / kTileX;
+  int px, py;
+  pixel_of_thread(px, py);
+  px += (blockIdx.x % tiles_x) * kTileX;
+  py += (blockIdx.x / tiles_x) * kTileY;
+  if (px >= p.W || py >= p.H) return;
+  const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  S* grad = reinterpret_cast<S*>(p.in_grad) + int64_t(b) * p.din.count() * CIN;
+  const Ray r = ray_setup(cam, px, py, p);
+  if (!r.hit || r.steps <= 0) return;
+  S G[CB];
+  const S* og = reinterpret_cast<const S*>(p.out_grad) + ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
+#pragma unroll
+  for (int k = 0; k < CB; ++k) G[k] = og[k];
+
+  if (!stateful<CB>(p.blend)) {
+    // stateless blends: the adjoint of each step needs only the cell itself
+    float pos[3] = {r.s[0], r.s[1], r.s[2]};
+    for (int i = 0; i < r.steps; ++i) {
+      S cell[CB], dcell[CB];
+      sample_cell<CIN, CB>(g, pos, p, cell);
+      blend_adjoint<CB>(G, cell, S(0), p.blend, dcell);
+      scatter_cell<CIN, CB>(p, grad, pos, dcell);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
+    }
+    return;
+  }
+
+  // segment length K (multiple of kSeg) so that at most kMaxCkpt checkpoints are needed
+  const int nseg_min = (r.steps + kMaxCkpt - 1) / kMaxCkpt;
+  const int K = ((max(nseg_min, kSeg) + kSeg - 1) / kSeg) * kSeg;
+  const int nck = (r.steps + K - 1) / K;
+  float ck_pos[kMaxCkpt][3];
+  S ck_a[kMaxCkpt];
+  {
+    float pos[3] = {r.s[0], r.s[1], r.s[2]};
+    S a = S(0);
+    for (int i = 0; i < r.steps; ++i) {
+      if (i % K == 0) {
+        const int k = i / K;
+        ck_pos[k][0] = pos[0];
+        ck_pos[k][1] = pos[1];
+        ck_pos[k][2] = pos[2];
+        ck_a[k] = a;
+      }
+      S cell[CB];
+      sample_cell<CIN, CB>(g, pos, p, cell);
+      a = state_update(a, cell[CB - 1], p.blend);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) pos[q] += r.st[q];
+    }
+  }
+  float buf_pos[kSeg][3];
+  S buf_cell[kSeg][CB];
+  S buf_a[kSeg];
+  for (int seg = nck - 1; seg >= 0; --seg) {
+    const int i0 = seg * K, i1 = min(i0 + K, r.steps);
+    const int nsub = (i1 - i0 + kSeg - 1) / kSeg;
+    for (int sub = nsub - 1; sub >= 0; --sub) {
+      const int j0 = i0 + sub * kSeg, j1 = min(j0 + kSeg, i1);
+      float pos[3] = {ck_pos[seg][0], ck_pos[seg][1], ck_pos[seg][2]};
+      S a = ck_a[seg];
+      for (int i = i0; i < j0; ++i) {  // re-march to the sub-segment start (only when K > kSeg)
+        S cell[CB];
+        sample_cell<CIN, CB>(g, pos, p, cell);
+        a = state_update(a, cell[CB - 1], p.blend);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) pos[q] += r.st[q];
+      }
+      for (int i = j0; i < j1; ++i) {
+        const int j = i - j0;
+        buf_pos[j][0] = pos[0];
+        buf_pos[j][1] = pos[1];
+        buf_pos[j][2] = pos[2];
+        buf_a[j] = a;
+        sample_cell<CIN, CB>(g, pos, p, buf_cell[j]);
+        a = state_update(a, buf_cell[j][CB - 1], p.blend);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) pos[q] += r.st[q];
+      }
+      for (int j = j1 - j0 - 1; j >= 0; --j) {
+        S dcell[CB];
+        blend_adjoint<CB>(G, buf_cell[j], buf_a[j], p.blend, dcell);
+        scatter_cell<CIN, CB>(p, grad, buf_pos[j], dcell);
+      }
+    }
+  }
+}
+
+// --------------------------------------------------- reference backward
+// scatterGrad3DInterpolated with per-voxel weight sums (sampling_v2.hpp:438-559)
+template <int C, class S>
+__device__ __forceinline__ void scatter_weighted(S* __restrict__ buf, S* __restrict__ wsum, S px, S py, S pz,
+                                                 const Dims& d, int bm, const S g[C]) {
+  if (bm == BORDER && !(px > S(-1) && px < S(d.x) && py > S(-1) && py < S(d.y) && pz > S(-1) && pz < S(d.z))) return;
+  Tri<S> t;
+  const S pp[3] = {px, py, pz};
+  const int n[3] = {d.x, d.y, d.z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const S f = floor(pp[a]);
+    t.w[a] = pp[a] - f;
+    int i0 = to_int_rz(f), i1 = to_int_rz(ceil(pp[a]));
+    bool ok0 = true, ok1 = true;
+    if (bm == BORDER) {
+      ok0 = i0 >= 0 && i0 < n[a];
+      ok1 = i1 >= 0 && i1 < n[a];
+    } else if (bm == CLAMP) {
+      i0 = min(max(i0, 0), n[a] - 1);
+      i1 = min(max(i1, 0), n[a] - 1);
+    } else {
+      i0 = wrap_index(i0, n[a]);
+      i1 = wrap_index(i1, n[a]);
+    }
+    t.i0[a] = i0;
+    t.i1[a] = i1;
+    t.ok0[a] = ok0;
+    t.ok1[a] = ok1;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    bool ok;
+    const int64_t i = tri_corner(t, k, d, ok);
+    if (!ok) continue;
+    const S w = tri_weight(t, k);
+#pragma unroll
+    for (int c = 0; c < C; ++c) atomic_add(buf + i * C + c, g[c] * w);
+    atomic_add(wsum + i, w);
+  }
+}
+
+template <int CIN, int CB, class T, class S>
+__global__ void __launch_bounds__(kThreads) k_raymarch_bwd_reference(RayParams p) {
+  __shared__ Cam cam;
+  int b, c, oslot;
+  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
+  if (threadIdx.x == 0) load_cam(p, b, c, cam);
+  __syncthreads();
+  const int tiles_x = (p.W + kTileX - 1) / kTileX;
+  int px, py;
+  pixel_of_thread(px, py);
+  px += (blockIdx.x % tiles_x) * kTileX;
+  py += (blockIdx.x / tiles_x) * kTileY;
+  if (px >= p.W || py >= p.H) return;
+  const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  S* buf = reinterpret_cast<S*>(p.wbuf);
+  S* wsum = reinterpret_cast<S*>(p.wsum);
+  const Ray r = ray_setup(cam, px, py, p);
+  if (!r.hit) return;
+  const int64_t o = ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
+  S G[CB], acc[CB];
+#pragma unroll
+  for (int k = 0; k < CB; ++k) {
+    G[k] = reinterpret_cast<const S*>(p.out_grad)[o + k];
+    acc[k] = reinterpret_cast<const S*>(p.out_fwd)[o + k];
+  }
+  float pos[3] = {r.e[0], r.e[1], r.e[2]};
+  for (int i = r.steps - 1; i >= 0; --i) {
+    S cell[CB], dcell[CB];
+    sample_cell<CIN, CB>(g, pos, p, cell);
+    blend_grad_reference<CB>(G, cell, acc, p.blend, dcell);
+    const S qx = S(pos[0] - 0.5f), qy = S(pos[1] - 0.5f), qz = S(pos[2] - 0.5f);
+    if (CIN == CB) {
+      S gg[CIN];
+#pragma unroll
+      for (int k = 0; k < CIN; ++k) gg[k] = dcell[k < CB ? k : 0];
+      scatter_weighted<CIN>(buf, wsum, qx, qy, qz, p.din, p.bm, gg);
+    } else {
+      S gg[1] = {S(0)};
+#pragma unroll
+      for (int k = 0; k < CB; ++k) gg[0] += S(p.scale[k]) * dcell[k];
+      scatter_weighted<1>(buf, wsum, qx, qy, qz, p.din, p.bm, gg);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pos[a] -= r.st[a];
+  }
+}
+
+// kNormalize3DGradients<T,SetZero,AddGrad> (raymarch_grid.cu.cc:458-480): add the
+// camera's buffered gradient divided by the summed weights, then clear both.
+template <int C, class S>
+__global__ void k_normalize_add(S* __restrict__ grad, S* __restrict__ buf, S* __restrict__ wsum, int64_t n) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const S w = wsum[i];
+  if (w > S(0)) {
+    const S inv = S(1) / w;
+#pragma unroll
+    for (int c = 0; c < C; ++c) grad[i * C + c] += buf[i * C + c] * inv;
+  }
+#pragma unroll
+  for (int c = 0; c < C; ++c) buf[i * C + c] = S(0);
+  wsum[i] = S(0);
+}
+
+// ------------------------------------------------------------- host side
+int validate(const ngt_raymarch_args* a, int& cin, int& cb) {
+  if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null arguments");
+  if (!positive_shape(a->input_shape, 5) || !positive_shape(a->output_dhw, 3))
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: shapes must be positive");
+  cin = int(a->input_shape[4]);
+  if (!valid_channels(cin)) return fail(NGT_ERR_INVALID_ARGUMENT, "Only 1,2 and 4 Channel supported.");
+  cb = cin;
+  if (a->emission_channels) {
+    if (cin != 1 || !(a->emission_channels == 2 || a->emission_channels == 4))
+      return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: emission expansion needs a 1-channel input and 2 or 4 channels");
+    cb = a->emission_channels;
+  }
+  if (!a->input || !a->output || !a->matrix_m || !a->matrix_v || !a->matrix_p || !a->frustum)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null pointer");
+  if (a->num_cameras <= 0) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: num_cameras must be positive");
+  if (!a->separate_camera_batch && a->num_cameras != a->input_shape[0])
+    return fail(NGT_ERR_INVALID_ARGUMENT, "camera batch must match data batch when not using global sampling.");
+  if (a->interpolation < NGT_NEAREST || a->interpolation > NGT_MAX)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: invalid interpolation");
+  if (a->boundary < NGT_BORDER || a->boundary > NGT_WRAP) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: invalid boundary");
+  if (!(a->blending_mode == NGT_BEER_LAMBERT || a->blending_mode == NGT_ALPHA ||
+        a->blending_mode == NGT_ALPHA_ADDITIVE || a->blending_mode == NGT_ADDITIVE))
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: invalid blending_mode");
+  if (a->dtype < NGT_F32 || a->dtype > NGT_F16) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: invalid dtype");
+  if (a->input_shape[1] > (1 << 30) || a->output_dhw[1] * a->output_dhw[2] > (int64_t(1) << 31))
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: shape too large");
+  return NGT_OK;
+}
+
+RayParams make_params(const ngt_raymarch_args* a) {
+  RayParams p = {};
+  p.input = a->input;
+  p.output = a->output;
+  p.M = a->matrix_m;
+  p.V = a->matrix_v;
+  p.P = a->matrix_p;
+  p.F = a->frustum;
+  p.din = Dims{int(a->input_shape[3]), int(a->input_shape[2]), int(a->input_shape[1])};
+  p.D = int(a->output_dhw[0]);
+  p.H = int(a->output_dhw[1]);
+  p.W = int(a->output_dhw[2]);
+  p.N = int(a->input_shape[0]);
+  p.ncam = a->num_cameras;
+  p.sep = a->separate_camera_batch ? 1 : 0;
+  p.fm = a->interpolation;
+  p.bm = a->boundary;
+  p.blend = a->blending_mode;
+  for (int i = 0; i < 4; ++i) p.scale[i] = a->emission_scale[i];
+  return p;
+}
+
+int num_slots(const RayParams& p) { return p.sep ? p.N * p.ncam : p.N; }
+
+template <template <int, int, class, class> class K, class T, class S>
+int dispatch_channels(int cin, int cb, dim3 grid, cudaStream_t st, const RayParams& p);
+
+enum Which { FWD = 0, BWD_EXACT = 1, BWD_REF = 2 };
+
+template <int CIN, int CB, class T, class S>
+void launch(int which, dim3 grid, cudaStream_t st, const RayParams& p) {
+  if (which == FWD)
+    k_raymarch_fwd<CIN, CB, T, S><<<grid, kThreads, 0, st>>>(p);
+  else if (which == BWD_EXACT)
+    k_raymarch_bwd_exact<CIN, CB, T, S><<<grid, kThreads, 0, st>>>(p);
+  else
+    k_raymarch_bwd_reference<CIN, CB, T, S><<<grid, kThreads, 0, st>>>(p);
+}
+
+template <class T, class S>
+int launch_typed(int which, int cin, int cb, dim3 grid, cudaStream_t st, const RayParams& p) {
+  if (cin == 1 && cb == 1) launch<1, 1, T, S>(which, grid, st, p);
+  else if (cin == 2 && cb == 2) launch<2, 2, T, S>(which, grid, st, p);
+  else if (cin == 4 && cb == 4) launch<4, 4, T, S>(which, grid, st, p);
+  else if (cin == 1 && cb == 2) launch<1, 2, T, S>(which, grid, st, p);
+  else if (cin == 1 && cb == 4) launch<1, 4, T, S>(which, grid, st, p);
+  else return fail(NGT_ERR_UNSUPPORTED, "raymarch: unsupported channel combination");
+  return NGT_OK;
+}
+
+int launch_dtype(int dtype, int which, int cin, int cb, dim3 grid, cudaStream_t st, const RayParams& p) {
+  switch (dtype) {
+    case NGT_F32: return launch_typed<float, float>(which, cin, cb, grid, st, p);
+    case NGT_F64: return launch_typed<double, double>(which, cin, cb, grid, st, p);
+    case NGT_BF16: return launch_typed<__nv_bfloat16, float>(which, cin, cb, grid, st, p);
+    case NGT_F16: return launch_typed<__half, float>(which, cin, cb, grid, st, p);
+  }
+  return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: invalid dtype");
+}
+
+size_t compute_size(int dtype) { return dtype == NGT_F64 ? 8 : 4; }
+
+}  // namespace
+}  // namespace ngt
+
+using namespace ngt;
+
+extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
+  int cin, cb;
+  int rc = validate(a, cin, cb);
+  if (rc) return rc;
+  RayParams p = make_params(a);
+  const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
+  const int slots = num_slots(p);
+  for (int s0 = 0; s0 < slots; s0 += 65535) {
+    p.slot0 = s0;
+    const dim3 grid(tiles, min(65535, slots - s0));
+    rc = launch_dtype(a->dtype, FWD, cin, cb, grid, as_stream(stream), p);
+    if (rc) return rc;
+  }
+  return check_launch("ngt_raymarch_fwd");
+}
+
+extern "C" size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* a) {
+  if (!a || a->grad_mode != NGT_GRAD_REFERENCE) return 0;
+  const int64_t vox = a->fwd.input_shape[1] * a->fwd.input_shape[2] * a->fwd.input_shape[3];
+  const int64_t cin = a->fwd.input_shape[4];
+  return size_t(vox * (cin + 1)) * compute_size(a->fwd.dtype);
+}
+
+extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
+  if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: null arguments");
+  int cin, cb;
+  int rc = validate(&a->fwd, cin, cb);
+  if (rc) return rc;
+  if (a->fwd.interpolation != NGT_LINEAR)
+    return fail(NGT_ERR_UNSUPPORTED, "raymarch gradients support LINEAR interpolation only");
+  if (!a->output_grad || !a->input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: null pointer");
+  if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: invalid grad_mode");
+  RayParams p = make_params(&a->fwd);
+  p.out_fwd = a->output;
+  p.out_grad = a->output_grad;
+  p.in_grad = a->input_grad;
+  cudaStream_t st = as_stream(stream);
+  const int64_t vox = p.din.count();
+  const size_t cs = compute_size(a->fwd.dtype);
+  if (cudaMemsetAsync(a->input_grad, 0, size_t(p.N) * vox * cin * cs, st) != cudaSuccess)
+    return check_launch("raymarch_bwd memset");
+  const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
+  const int slots = num_slots(p);
+  if (a->grad_mode == NGT_GRAD_EXACT) {
+    for (int s0 = 0; s0 < slots; s0 += 65535) {
+      p.slot0 = s0;
+      const dim3 grid(tiles, min(65535, slots - s0));
+      rc = launch_dtype(a->fwd.dtype, BWD_EXACT, cin, cb, grid, st, p);
+      if (rc) return rc;
+    }
+    return check_launch("ngt_raymarch_bwd");
+  }
+  // reference: one (batch, camera) at a time, normalised by summed weights per camera
+  if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: reference mode needs the forward output");
+  const size_t need = ngt_raymarch_bwd_workspace_bytes(a);
+  if (!a->workspace || a->workspace_bytes < need)
+    return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: reference mode needs %zu workspace bytes", need);
+  p.wbuf = a->workspace;
+  p.wsum = static_cast<char*>(a->workspace) + size_t(vox * cin) * cs;
+  if (cudaMemsetAsync(a->workspace, 0, need, st) != cudaSuccess) return check_launch("raymarch_bwd memset");
+  for (int s = 0; s < slots; ++s) {
+    p.slot0 = s;
+    const int b = p.sep ? s / p.ncam : s;
+    rc = launch_dtype(a->fwd.dtype, BWD_REF, cin, cb, dim3(tiles, 1), st, p);
+    if (rc) return rc;
+    const unsigned nb = ceil_div_u(vox, 256);
+    if (a->fwd.dtype == NGT_F64) {
+      double* gr = static_cast<double*>(a->input_grad) + int64_t(b) * vox * cin;
+      if (cin == 1) k_normalize_add<1, double><<<nb, 256, 0, st>>>(gr, (double*)p.wbuf, (double*)p.wsum, vox);
+      else if (cin == 2) k_normalize_add<2, double><<<nb, 256, 0, st>>>(gr, (double*)p.wbuf, (double*)p.wsum, vox);
+      else k_normalize_add<4, double><<<nb, 256, 0, st>>>(gr, (double*)p.wbuf, (double*)p.wsum, vox);
+    } else {
+      float* gr = static_cast<float*>(a->input_grad) + int64_t(b) * vox * cin;
+      if (cin == 1) k_normalize_add<1, float><<<nb, 256, 0, st>>>(gr, (float*)p.wbuf, (float*)p.wsum, vox);
+      else if (cin == 2) k_normalize_add<2, float><<<nb, 256, 0, st>>>(gr, (float*)p.wbuf, (float*)p.wsum, vox);
+      else k_normalize_add<4, float><<<nb, 256, 0, st>>>(gr, (float*)p.wbuf, (float*)p.wsum, vox);
+    }
+  }
+  return check_launch("ngt_raymarch_bwd");
+}

@@ -1,0 +1,58 @@
+// Image L2 loss of the reconstruction step: gradient of 0.5*||image - target||^2
+// on the first loss_channels channels, and the loss reduced per block then
+// added atomically.
+#include "ngt_common.cuh"
+#include "ngt_host.cuh"
+
+namespace ngt {
+namespace {
+
+constexpr int kBlock = 256;
+
+template <class S>
+__global__ void __launch_bounds__(kBlock) k_l2(int64_t pixels, int C, int LC, const S* __restrict__ img,
+                                               const S* __restrict__ tgt, S* __restrict__ grad, float* loss) {
+  __shared__ float part[kBlock / 32];
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  float acc = 0.0f;
+  if (i < pixels) {
+    for (int c = 0; c < C; ++c) {
+      S g = S(0);
+      if (c < LC) {
+        g = img[i * C + c] - tgt[i * LC + c];
+        acc += float(g) * float(g);
+      }
+      grad[i * C + c] = g;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < kBlock / 32 ? part[threadIdx.x] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) atomicAdd(loss, 0.5f * v);
+  }
+}
+
+}  // namespace
+}  // namespace ngt
+
+using namespace ngt;
+
+extern "C" int ngt_image_l2_loss(int32_t dtype, int64_t pixels, int32_t channels, int32_t loss_channels,
+                                 const void* image, const void* target, void* image_grad, float* loss, void* stream) {
+  if (!image || !target || !image_grad || !loss) return fail(NGT_ERR_INVALID_ARGUMENT, "image_l2_loss: null pointer");
+  if (pixels <= 0 || channels <= 0 || loss_channels <= 0 || loss_channels > channels)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "image_l2_loss: invalid sizes");
+  const unsigned nb = ceil_div_u(pixels, kBlock);
+  if (dtype == NGT_F64)
+    k_l2<double><<<nb, kBlock, 0, as_stream(stream)>>>(pixels, channels, loss_channels, (const double*)image,
+                                                        (const double*)target, (double*)image_grad, loss);
+  else if (dtype == NGT_F32)
+    k_l2<float><<<nb, kBlock, 0, as_stream(stream)>>>(pixels, channels, loss_channels, (const float*)image,
+                                                       (const float*)target, (float*)image_grad, loss);
+  else
+    return fail(NGT_ERR_UNSUPPORTED, "image_l2_loss: images are F32 or F64");
+  return check_launch("ngt_image_l2_loss");
+}

@@ -1,0 +1,460 @@
+"""The grid operators with the reference's call signatures.
+
+Mirrors ``sampling_ops``, ``raymarching_ops`` and ``blending_ops`` of
+``phitest/render/cuda/ops_loader.py``: the same keyword names and attribute
+strings, NDHWC tensors, matrices as 16 floats read column-major (callers pass
+``matrix.transpose()`` exactly as ``renderer.py:117-121`` does).  Every forward
+is a ``torch.autograd.Function`` whose backward is the matching gradient op, so
+``torch.autograd`` plays the role of the gradients registered in ops_loader.py.
+
+Gradient semantics: ``set_gradient_mode("exact")`` (default, the true adjoint)
+or ``"reference"`` (the reference's count / weight normalised gradients).
+
+All tensors must be contiguous CUDA tensors; there is no CPU path.
+"""
+import contextlib
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+_GRAD_MODE = ["exact"]
+
+
+def set_gradient_mode(mode):
+    if mode not in L.GRAD:
+        raise ValueError("gradient mode must be 'exact' or 'reference'")
+    _GRAD_MODE[0] = mode
+
+
+def get_gradient_mode():
+    return _GRAD_MODE[0]
+
+
+@contextlib.contextmanager
+def gradient_mode(mode):
+    old = get_gradient_mode()
+    set_gradient_mode(mode)
+    try:
+        yield
+    finally:
+        set_gradient_mode(old)
+
+
+# ------------------------------------------------------------------ helpers
+_DTYPES = {torch.float32: L.F32, torch.float64: L.F64, torch.bfloat16: L.BF16, torch.float16: L.F16}
+
+
+def _code(t):
+    if t.dtype not in _DTYPES:
+        raise TypeError("unsupported dtype %s" % t.dtype)
+    return _DTYPES[t.dtype]
+
+
+def compute_dtype(t):
+    return torch.float64 if t.dtype == torch.float64 else torch.float32
+
+
+def _cuda(t, name):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise ValueError("%s must be a CUDA tensor (the operators have no CPU path)" % name)
+    return t.contiguous()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _enum(table, value, name):
+    v = value.decode() if isinstance(value, bytes) else value
+    if v not in table:
+        raise ValueError("invalid %s '%s'" % (name, value))
+    return table[v]
+
+
+def _floats(m, width, device):
+    """Matrices / frusta as the contiguous float32 device buffer the kernels read:
+    the C-order flattening of what the caller passed, ``width`` floats per entry."""
+    if isinstance(m, torch.Tensor):
+        t = m.detach().to(device=device, dtype=torch.float32)
+    else:
+        t = torch.as_tensor(np.asarray(m, dtype=np.float32), device=device)
+    return t.reshape(-1, width).contiguous()
+
+
+def _workspace(nbytes, device):
+    if nbytes == 0:
+        return None
+    return torch.empty(int(nbytes), dtype=torch.uint8, device=device)
+
+
+def _shape5(t):
+    return L.I64x5(*[int(s) for s in t.shape])
+
+
+# ------------------------------------------------------------------ LUT resample
+def _lut_args(input, lookup, output, a):
+    args = L.SampleLutArgs()
+    args.dtype = _code(input)
+    args.input_shape = _shape5(input)
+    args.lookup_shape = _shape5(lookup)
+    args.input, args.lookup, args.output = _ptr(input), _ptr(lookup), _ptr(output)
+    args.interpolation = _enum(L.INTERP, a["interpolation"], "interpolation")
+    args.boundary = _enum(L.BOUNDARY, a["boundary"], "boundary")
+    args.mipmapping = _enum(L.MIP, a["mipmapping"], "mipmapping")
+    args.num_mipmaps = int(a["num_mipmaps"])
+    args.mip_bias = float(a["mip_bias"])
+    args.cell_center_offset = float(a["cell_center_offset"])
+    args.separate_camera_batch = int(bool(a["separate_camera_batch"]))
+    args.relative_coords = int(bool(a["relative_coords"]))
+    args.normalized_coords = int(bool(a["normalized_coords"]))
+    return args
+
+
+def _lut_forward(input, lookup, a):
+    N, C = input.shape[0], input.shape[-1]
+    V = lookup.shape[0]
+    out = torch.empty((N, V if a["separate_camera_batch"] else 1) + tuple(lookup.shape[1:4]) + (C,),
+                      dtype=input.dtype, device=input.device)
+    args = _lut_args(input, lookup, out, a)
+    ws = _workspace(L.load().ngt_sample_lut_fwd_workspace_bytes(ctypes.byref(args)), input.device)
+    args.workspace, args.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
+    L.call("ngt_sample_lut_fwd", ctypes.byref(args), _stream())
+    return out
+
+
+def _lut_backward(input, output_grad, lookup, a, mode):
+    g = L.SampleLutGradArgs()
+    g.fwd = _lut_args(input, lookup, None, a)
+    input_grad = torch.empty_like(input)
+    lookup_grad = torch.empty_like(lookup)
+    g.output_grad, g.input_grad, g.lookup_grad = _ptr(output_grad), _ptr(input_grad), _ptr(lookup_grad)
+    g.grad_mode = L.GRAD[mode]
+    ws = _workspace(L.load().ngt_sample_lut_bwd_workspace_bytes(ctypes.byref(g)), input.device)
+    g.workspace, g.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
+    L.call("ngt_sample_lut_bwd", ctypes.byref(g), _stream())
+    return input_grad, lookup_grad
+
+
+class _SampleGridLut(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, input, lookup, attrs):
+        ctx.attrs = attrs
+        ctx.mode = get_gradient_mode()
+        ctx.save_for_backward(input, lookup)
+        return _lut_forward(input, lookup, attrs)
+
+    @staticmethod
+    def backward(ctx, grad):
+        input, lookup = ctx.saved_tensors
+        gi, gl = _lut_backward(input, grad.contiguous(), lookup, ctx.attrs, ctx.mode)
+        return gi, gl, None
+
+
+def sample_grid_lut(input, lookup, interpolation="LINEAR", boundary="BORDER", mipmapping="NONE", num_mipmaps=0,
+                    mip_bias=0.0, coordinate_mode="LOOKUP", cell_center_offset=0.0, separate_camera_batch=True,
+                    relative_coords=True, normalized_coords=False):
+    """``SampleGridLut`` (resample_grid.cc:94-120): input NDHWC, lookup VDHW4 (x, y, z,
+    LoD) -> NVDHWC.  Differentiable w.r.t. input and lookup."""
+    if coordinate_mode != "LOOKUP":
+        raise ValueError("Invalid coorindate_mode")
+    input = _cuda(input, "input")
+    lookup = _cuda(lookup, "lookup").to(input.dtype)
+    attrs = dict(interpolation=interpolation, boundary=boundary, mipmapping=mipmapping, num_mipmaps=num_mipmaps,
+                 mip_bias=mip_bias, cell_center_offset=cell_center_offset,
+                 separate_camera_batch=separate_camera_batch, relative_coords=relative_coords,
+                 normalized_coords=normalized_coords)
+    return _SampleGridLut.apply(input, lookup, attrs)
+
+
+def sample_grid_lut_grad(input, output_grad, lookup, interpolation="LINEAR", boundary="BORDER", mipmapping="NONE",
+                         num_mipmaps=0, mip_bias=0.0, coordinate_mode="LOOKUP", cell_center_offset=0.0,
+                         separate_camera_batch=True, relative_coords=True, normalized_coords=False, grad_mode=None):
+    """``SampleGridLutGrad`` (resample_grid.cc:124-150): returns (input_grad, lookup_grad)."""
+    input = _cuda(input, "input")
+    attrs = dict(interpolation=interpolation, boundary=boundary, mipmapping=mipmapping, num_mipmaps=num_mipmaps,
+                 mip_bias=mip_bias, cell_center_offset=cell_center_offset,
+                 separate_camera_batch=separate_camera_batch, relative_coords=relative_coords,
+                 normalized_coords=normalized_coords)
+    return _lut_backward(input, _cuda(output_grad, "output_grad").to(input.dtype),
+                         _cuda(lookup, "lookup").to(input.dtype), attrs, grad_mode or get_gradient_mode())
+
+
+# ------------------------------------------------------------ transform resample
+def _xf_args(input, M, V, P, F, out_dhw, output, a):
+    args = L.SampleTransformArgs()
+    args.dtype = _code(input)
+    args.input_shape = _shape5(input)
+    args.output_dhw = L.I64x3(*[int(s) for s in out_dhw])
+    args.input, args.output = _ptr(input), _ptr(output)
+    args.matrix_m, args.matrix_v, args.matrix_p, args.frustum = _ptr(M), _ptr(V), _ptr(P), _ptr(F)
+    args.num_cameras = V.shape[0]
+    args.interpolation = _enum(L.INTERP, a["interpolation"], "interpolation")
+    args.boundary = _enum(L.BOUNDARY, a["boundary"], "boundary")
+    args.mipmapping = _enum(L.MIP, a["mipmapping"], "mipmapping")
+    args.num_mipmaps = int(a["num_mipmaps"])
+    args.mip_bias = float(a["mip_bias"])
+    args.cell_center_offset = float(a["cell_center_offset"])
+    args.coordinate_mode = _enum(L.COORD, a["coordinate_mode"], "coordinate_mode")
+    args.separate_camera_batch = int(bool(a["separate_camera_batch"]))
+    return args
+
+
+class _SampleGridTransform(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, input, M, V, P, F, out_dhw, attrs):
+        N, C = input.shape[0], input.shape[-1]
+        out = torch.empty((N, V.shape[0] if attrs["separate_camera_batch"] else 1) + tuple(out_dhw) + (C,),
+                          dtype=input.dtype, device=input.device)
+        args = _xf_args(input, M, V, P, F, out_dhw, out, attrs)
+        ws = _workspace(L.load().ngt_sample_transform_fwd_workspace_bytes(ctypes.byref(args)), input.device)
+        args.workspace, args.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
+        L.call("ngt_sample_transform_fwd", ctypes.byref(args), _stream())
+        ctx.save_for_backward(input, M, V, P, F)
+        ctx.attrs, ctx.out_dhw, ctx.mode = attrs, out_dhw, get_gradient_mode()
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        input, M, V, P, F = ctx.saved_tensors
+        gi = _xf_backward(input, grad.contiguous(), M, V, P, F, ctx.out_dhw, ctx.attrs, ctx.mode)
+        return gi, None, None, None, None, None, None
+
+
+def _xf_backward(input, output_grad, M, V, P, F, out_dhw, a, mode):
+    g = L.SampleTransformGradArgs()
+    g.fwd = _xf_args(input, M, V, P, F, out_dhw, None, a)
+    gi = torch.empty_like(input)
+    g.output_grad, g.input_grad, g.grad_mode = _ptr(output_grad), _ptr(gi), L.GRAD[mode]
+    ws = _workspace(L.load().ngt_sample_transform_bwd_workspace_bytes(ctypes.byref(g)), input.device)
+    g.workspace, g.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
+    L.call("ngt_sample_transform_bwd", ctypes.byref(g), _stream())
+    return gi
+
+
+def _xf_prepare(input, matrix_m, matrix_v, matrix_p, frustum_params):
+    input = _cuda(input, "input")
+    dev = input.device
+    return input, _floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev), \
+        _floats(frustum_params, 6, dev)
+
+
+def sample_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape, interpolation="LINEAR",
+                          boundary="BORDER", mipmapping="NONE", num_mipmaps=0, mip_bias=0.0,
+                          coordinate_mode="TRANSFORM_LINDEPTH", cell_center_offset=0.5, separate_camera_batch=True):
+    """``SampleGridTransform`` (resample_grid.cc:23-65): input NDHWC -> NVDHWC with
+    DHW = output_shape, sampled through model / view / projection / frustum."""
+    input, M, V, P, F = _xf_prepare(input, matrix_m, matrix_v, matrix_p, frustum_params)
+    attrs = dict(interpolation=interpolation, boundary=boundary, mipmapping=mipmapping, num_mipmaps=num_mipmaps,
+                 mip_bias=mip_bias, coordinate_mode=coordinate_mode, cell_center_offset=cell_center_offset,
+                 separate_camera_batch=separate_camera_batch)
+    out_dhw = tuple(int(s) for s in list(output_shape)[:3])
+    return _SampleGridTransform.apply(input, M, V, P, F, out_dhw, attrs)
+
+
+def sample_grid_transform_grad(input, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,
+                               interpolation="LINEAR", boundary="BORDER", mipmapping="NONE", num_mipmaps=0,
+                               mip_bias=0.0, coordinate_mode="TRANSFORM_LINDEPTH", cell_center_offset=0.5,
+                               separate_camera_batch=True, grad_mode=None):
+    """``SampleGridTransformGrad`` (resample_grid.cc:68-92)."""
+    input, M, V, P, F = _xf_prepare(input, matrix_m, matrix_v, matrix_p, frustum_params)
+    output_grad = _cuda(output_grad, "output_grad").to(input.dtype)
+    attrs = dict(interpolation=interpolation, boundary=boundary, mipmapping=mipmapping, num_mipmaps=num_mipmaps,
+                 mip_bias=mip_bias, coordinate_mode=coordinate_mode, cell_center_offset=cell_center_offset,
+                 separate_camera_batch=separate_camera_batch)
+    return _xf_backward(input, output_grad, M, V, P, F, tuple(output_grad.shape[2:5]), attrs,
+                        grad_mode or get_gradient_mode())
+
+
+def lod_transform(input_shape, matrix_mv, matrix_p, frustum_params, output_shape, inverse_transform=False,
+                  linearize_depth=True, relative_coords=False, device="cuda"):
+    """``LodTransform`` (resample_grid.cc:152-172): per camera a (V, D', H', W', 4)
+    float32 lookup table of sampling positions and level of detail."""
+    MV, P, F = _floats(matrix_mv, 16, device), _floats(matrix_p, 16, device), _floats(frustum_params, 6, device)
+    out_dhw = [int(s) for s in list(output_shape)[:3]]
+    out = torch.empty([MV.shape[0]] + out_dhw + [4], dtype=torch.float32, device=device)
+    a = L.LodArgs()
+    a.input_dhw = L.I64x3(*[int(s) for s in list(input_shape)[:3]])
+    a.output_dhw = L.I64x3(*out_dhw)
+    a.matrix_mv, a.matrix_p, a.frustum = _ptr(MV), _ptr(P), _ptr(F)
+    a.num_cameras = MV.shape[0]
+    a.inverse_transform, a.linearize_depth, a.relative_coords = int(inverse_transform), int(linearize_depth), \
+        int(relative_coords)
+    a.output = _ptr(out)
+    L.call("ngt_lod_transform", ctypes.byref(a), _stream())
+    return out
+
+
+def mip_pyramid(input, levels):
+    """Mip levels 1..levels of an NDHWC grid (box filter, as the resample op's
+    mip atlas), returned as a list of tensors."""
+    input = _cuda(input, "input")
+    shape = L.I64x5(*[int(s) for s in input.shape])
+    nbytes = L.load().ngt_mip_bytes(_code(input), shape, int(levels))
+    ws = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=input.device)
+    L.call("ngt_mip_build", _code(input), shape, _ptr(input), int(levels), _ptr(ws), ctypes.c_size_t(nbytes),
+           _stream())
+    out, off = [], 0
+    es = input.element_size()
+    for lv in range(1, int(levels) + 1):
+        s = [input.shape[0], input.shape[1] >> lv, input.shape[2] >> lv, input.shape[3] >> lv, input.shape[4]]
+        n = int(np.prod(s))
+        out.append(ws[off:off + n * es].view(input.dtype).view(s).clone())
+        off += (n * es + 255) // 256 * 256
+    return out
+
+
+# ------------------------------------------------------------------ raymarch
+def _ray_args(input, M, V, P, F, out_dhw, output, a):
+    r = L.RaymarchArgs()
+    r.dtype = _code(input)
+    r.input_shape = _shape5(input)
+    r.output_dhw = L.I64x3(*[int(s) for s in out_dhw])
+    r.input, r.output = _ptr(input), _ptr(output)
+    r.matrix_m, r.matrix_v, r.matrix_p, r.frustum = _ptr(M), _ptr(V), _ptr(P), _ptr(F)
+    r.num_cameras = V.shape[0]
+    r.interpolation = _enum(L.INTERP, a["interpolation"], "interpolation")
+    r.boundary = _enum(L.BOUNDARY, a["boundary"], "boundary")
+    r.blending_mode = _enum(L.BLEND, a["blending_mode"], "blending_mode")
+    r.keep_dims = int(bool(a["keep_dims"]))
+    r.separate_camera_batch = int(bool(a["separate_camera_batch"]))
+    es = a.get("emission_scale")
+    if es is not None:
+        r.emission_channels = len(es)
+        for i, v in enumerate(es):
+            r.emission_scale[i] = float(v)
+    return r
+
+
+def _ray_out_shape(input, V, out_dhw, a):
+    N = input.shape[0]
+    nv = V.shape[0] if a["separate_camera_batch"] else 1
+    cb = len(a["emission_scale"]) if a.get("emission_scale") is not None else input.shape[-1]
+    shape = (N, nv, int(out_dhw[1]), int(out_dhw[2]), cb)
+    return shape if not a["keep_dims"] else (N, nv, 1) + shape[2:]
+
+
+def _ray_forward(input, M, V, P, F, out_dhw, a):
+    out = torch.empty(_ray_out_shape(input, V, out_dhw, a), dtype=compute_dtype(input), device=input.device)
+    r = _ray_args(input, M, V, P, F, out_dhw, out, a)
+    L.call("ngt_raymarch_fwd", ctypes.byref(r), _stream())
+    return out
+
+
+def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode):
+    g = L.RaymarchGradArgs()
+    g.fwd = _ray_args(input, M, V, P, F, out_dhw, None, a)
+    gi = torch.empty(input.shape, dtype=compute_dtype(input), device=input.device)
+    g.output, g.output_grad, g.input_grad, g.grad_mode = _ptr(output), _ptr(output_grad), _ptr(gi), L.GRAD[mode]
+    ws = _workspace(L.load().ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g)), input.device)
+    g.workspace, g.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
+    L.call("ngt_raymarch_bwd", ctypes.byref(g), _stream())
+    return gi
+
+
+class _RaymarchGridTransform(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, input, M, V, P, F, out_dhw, attrs):
+        out = _ray_forward(input, M, V, P, F, out_dhw, attrs)
+        ctx.save_for_backward(input, M, V, P, F, out)
+        ctx.attrs, ctx.out_dhw, ctx.mode = attrs, out_dhw, get_gradient_mode()
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        input, M, V, P, F, out = ctx.saved_tensors
+        gi = _ray_backward(input, out, grad.contiguous().to(out.dtype), M, V, P, F, ctx.out_dhw, ctx.attrs, ctx.mode)
+        return gi, None, None, None, None, None, None
+
+
+def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape, interpolation="LINEAR",
+                            boundary="BORDER", blending_mode="BEER_LAMBERT", keep_dims=False,
+                            separate_camera_batch=True, emission_scale=None):
+    """``RaymarchGridTransform`` (raymarch_grid.cc:29-63): input NDHWC -> NVHWC
+    (NV1HWC with keep_dims); output_shape = (depth samples, H, W).
+
+    ``emission_scale`` (2 or 4 floats) is an extension for a 1-channel density
+    input: the blend then sees channel c = emission_scale[c] * density, the
+    renderer's ``[light*step, density*step]`` grid (renderer.py:533-548,763)
+    formed inside the kernel instead of materialised."""
+    input = _cuda(input, "input")
+    dev = input.device
+    M, V, P, F = (_floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev),
+                  _floats(frustum_params, 6, dev))
+    attrs = dict(interpolation=interpolation, boundary=boundary, blending_mode=blending_mode, keep_dims=keep_dims,
+                 separate_camera_batch=separate_camera_batch,
+                 emission_scale=None if emission_scale is None else tuple(float(v) for v in emission_scale))
+    out_dhw = tuple(int(s) for s in list(output_shape)[:3])
+    return _RaymarchGridTransform.apply(input, M, V, P, F, out_dhw, attrs)
+
+
+def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,
+                                 output_shape, interpolation="LINEAR", boundary="BORDER",
+                                 blending_mode="BEER_LAMBERT", keep_dims=False, separate_camera_batch=True,
+                                 grad_mode=None, emission_scale=None):
+    """``RaymarchGridTransformGrad`` (raymarch_grid.cc:67-92): the input gradient."""
+    input = _cuda(input, "input")
+    dev = input.device
+    M, V, P, F = (_floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev),
+                  _floats(frustum_params, 6, dev))
+    attrs = dict(interpolation=interpolation, boundary=boundary, blending_mode=blending_mode, keep_dims=keep_dims,
+                 separate_camera_batch=separate_camera_batch,
+                 emission_scale=None if emission_scale is None else tuple(float(v) for v in emission_scale))
+    cd = compute_dtype(input)
+    return _ray_backward(input, _cuda(output, "output").to(cd), _cuda(output_grad, "output_grad").to(cd), M, V, P, F,
+                         tuple(int(s) for s in list(output_shape)[:3]), attrs, grad_mode or get_gradient_mode())
+
+
+# -------------------------------------------------------------- reduce blend
+def _rb_args(input, output, blending_mode, keep_dims):
+    a = L.ReduceBlendArgs()
+    a.dtype = _code(input)
+    a.input_shape = _shape5(input)
+    a.input, a.output = _ptr(input), _ptr(output)
+    a.blending_mode = _enum(L.BLEND, blending_mode, "blending_mode")
+    a.keep_dims = int(bool(keep_dims))
+    return a
+
+
+def _rb_backward(output_grad, output, input, blending_mode, keep_dims, mode):
+    g = L.ReduceBlendGradArgs()
+    g.fwd = _rb_args(input, None, blending_mode, keep_dims)
+    gi = torch.empty_like(input)
+    g.output, g.output_grad, g.input_grad, g.grad_mode = _ptr(output), _ptr(output_grad), _ptr(gi), L.GRAD[mode]
+    L.call("ngt_reduce_blend_bwd", ctypes.byref(g), _stream())
+    return gi
+
+
+class _ReduceGridBlend(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, input, blending_mode, keep_dims):
+        N, D, H, W, C = input.shape
+        out = torch.empty((N, D, H, W, C) if keep_dims else (N, H, W, C), dtype=input.dtype, device=input.device)
+        L.call("ngt_reduce_blend_fwd", ctypes.byref(_rb_args(input, out, blending_mode, keep_dims)), _stream())
+        ctx.save_for_backward(input, out)
+        ctx.blend, ctx.keep, ctx.mode = blending_mode, keep_dims, get_gradient_mode()
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        input, out = ctx.saved_tensors
+        return _rb_backward(grad.contiguous(), out, input, ctx.blend, ctx.keep, ctx.mode), None, None
+
+
+def reduce_grid_blend(input, blending_mode="BEER_LAMBERT", keep_dims=False):
+    """``ReduceGridBlend`` (reduce_blend.cc:24-35): front-to-back blend along D."""
+    return _ReduceGridBlend.apply(_cuda(input, "input"), blending_mode, keep_dims)
+
+
+def reduce_grid_blend_grad(output_grad, output, input, blending_mode="BEER_LAMBERT", keep_dims=False,
+                           grad_mode=None):
+    """``ReduceGridBlendGrad`` (reduce_blend.cc:38-56)."""
+    input = _cuda(input, "input")
+    return _rb_backward(_cuda(output_grad, "output_grad").to(input.dtype), _cuda(output, "output").to(input.dtype),
+                        input, blending_mode, keep_dims, grad_mode or get_gradient_mode())

@@ -1,0 +1,141 @@
+"""One differentiated reconstruction step on device-resident tensors.
+
+The step of the density / velocity optimisation (optimization.py:1018-1046 and
+1263-1281 around State.render_density / VelocityGrid.warp):
+
+    rho' = MacCormack(rho, u)                        (warp, MC_SMOOTH, CLAMP)
+    image_v = raymarch(rho' as [light*step, step])    (Beer-Lambert, BORDER)
+    loss = 0.5 * sum_v ||image_v.light - target_v||^2
+    backward to rho and to the three MAC face grids
+
+The ambient light grid ``rho*c*i`` (lighting.py:26-34) and the step
+premultiply (renderer.py:533-548) are linear in rho, so the raymarch reads the
+one-channel rho' and forms both blend channels in registers; its gradient comes
+back as one channel.  All launches go through the C ABI with argument structs
+built once; ``capture()`` records the whole step as one CUDA graph.
+"""
+import ctypes
+
+import torch
+
+from . import _lib as L
+from .ops import _code, _ptr
+
+
+class RenderAdvectStep:
+    KERNELS_PER_STEP = 8  # advect 2, raymarch fwd, loss, raymarch bwd, advect bwd 3
+
+    def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
+                 clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact"):
+        dev = rho.device
+        self.lib = L.load()
+        self.rho, self.ux, self.uy, self.uz = rho.contiguous(), ux.contiguous(), uy.contiguous(), uz.contiguous()
+        self.M = torch.as_tensor(M, dtype=torch.float32, device=dev).reshape(-1, 16).contiguous()
+        self.V = torch.as_tensor(V, dtype=torch.float32, device=dev).reshape(-1, 16).contiguous()
+        self.P = torch.as_tensor(P, dtype=torch.float32, device=dev).reshape(-1, 16).contiguous()
+        self.F = torch.as_tensor(F, dtype=torch.float32, device=dev).reshape(-1, 6).contiguous()
+        self.targets = targets.to(device=dev, dtype=torch.float32).contiguous()
+        D, H, W = rho.shape[:3]
+        nv = self.V.shape[0]
+        dd, hh, ww = image_dhw
+        Fh = self.F.cpu()
+        depth_step = float(Fh[0, 1] - Fh[0, 0]) / dd
+        self.emission = (light * depth_step, depth_step)
+        st = rho.dtype
+        f32 = torch.float32
+        self.rho_adv = torch.empty((D, H, W, 1), dtype=st, device=dev)
+        self.fwd_field = torch.empty((D, H, W, 1), dtype=f32, device=dev)
+        self.image = torch.empty((1, nv, hh, ww, 2), dtype=f32, device=dev)
+        self.g_image = torch.empty_like(self.image)
+        self.g_rho_adv = torch.empty((D, H, W, 1), dtype=f32, device=dev)
+        self.g_rho = torch.empty((D, H, W, 1), dtype=f32, device=dev)
+        self.g_ux = torch.empty(ux.shape, dtype=f32, device=dev)
+        self.g_uy = torch.empty(uy.shape, dtype=f32, device=dev)
+        self.g_uz = torch.empty(uz.shape, dtype=f32, device=dev)
+        self.loss = torch.zeros((1,), dtype=f32, device=dev)
+        self.pixels = nv * hh * ww
+
+        a = L.AdvectArgs()
+        a.dtype = _code(rho)
+        a.grid_dhw = L.I64x3(D, H, W)
+        a.channels = 1
+        a.data, a.vel_x, a.vel_y, a.vel_z = _ptr(self.rho), _ptr(self.ux), _ptr(self.uy), _ptr(self.uz)
+        a.dt, a.order, a.clamp, a.boundary = float(dt), int(order), L.CLAMP[clamp], L.BOUNDARY[advect_boundary]
+        a.output, a.fwd_field = _ptr(self.rho_adv), _ptr(self.fwd_field)
+        self.adv = a
+        ag = L.AdvectGradArgs()
+        ag.fwd = a
+        ag.output_grad, ag.data_grad = _ptr(self.g_rho_adv), _ptr(self.g_rho)
+        ag.vel_x_grad, ag.vel_y_grad, ag.vel_z_grad = _ptr(self.g_ux), _ptr(self.g_uy), _ptr(self.g_uz)
+        ag.grad_mode = L.GRAD[grad_mode]
+        self.adv_ws = torch.empty(int(self.lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(ag))),
+                                  dtype=torch.uint8, device=dev)
+        ag.workspace, ag.workspace_bytes = _ptr(self.adv_ws), self.adv_ws.numel()
+        self.adv_g = ag
+
+        r = L.RaymarchArgs()
+        r.dtype = _code(rho)
+        r.input_shape = L.I64x5(1, D, H, W, 1)
+        r.output_dhw = L.I64x3(dd, hh, ww)
+        r.input, r.output = _ptr(self.rho_adv), _ptr(self.image)
+        r.matrix_m, r.matrix_v, r.matrix_p, r.frustum = _ptr(self.M), _ptr(self.V), _ptr(self.P), _ptr(self.F)
+        r.num_cameras = nv
+        r.interpolation, r.boundary = L.INTERP["LINEAR"], L.BOUNDARY[render_boundary]
+        r.blending_mode, r.keep_dims, r.separate_camera_batch = L.BLEND["BEER_LAMBERT"], 0, 1
+        r.emission_channels = 2
+        r.emission_scale[0], r.emission_scale[1] = self.emission
+        self.ray = r
+        rg = L.RaymarchGradArgs()
+        rg.fwd = r
+        rg.output, rg.output_grad, rg.input_grad = _ptr(self.image), _ptr(self.g_image), _ptr(self.g_rho_adv)
+        rg.grad_mode = L.GRAD[grad_mode]
+        self.ray_ws = None
+        nb = int(self.lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(rg)))
+        if nb:
+            self.ray_ws = torch.empty(nb, dtype=torch.uint8, device=dev)
+            rg.workspace, rg.workspace_bytes = _ptr(self.ray_ws), nb
+        self.ray_g = rg
+        self.graph = None
+
+    def _call(self, name, *args):
+        rc = getattr(self.lib, name)(*args)
+        if rc != L.NGT_OK:
+            raise L.NGTError(rc, self.lib.ngt_last_error_message().decode(errors="replace"))
+
+    def forward(self, stream=None):
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream if stream is None else stream)
+        self._call("ngt_advect_maccormack_fwd", ctypes.byref(self.adv), s)
+        self._call("ngt_raymarch_fwd", ctypes.byref(self.ray), s)
+
+    def launch(self):
+        """Enqueue forward + loss + backward on the current stream."""
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self.loss.zero_()
+        self.forward(s.value)
+        self._call("ngt_image_l2_loss", L.F32, self.pixels, 2, 1, _ptr(self.image), _ptr(self.targets),
+                   _ptr(self.g_image), _ptr(self.loss), s)
+        self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g), s)
+        self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_g), s)
+
+    def capture(self):
+        """Record one step as a CUDA graph (warm-up launch on a side stream first)."""
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.launch()
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.launch()
+        return self.graph
+
+    def step(self):
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.launch()
+        return self.loss
+
+    def gradients(self):
+        return self.g_rho, self.g_ux, self.g_uy, self.g_uz

@@ -1,0 +1,62 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+Stand-ins for the ScalarFlow captures (not available offline): Gaussian-blob
+densities, curl-noise MAC velocities and an orbit of cameras built with the
+reference's camera / grid-transform conventions (``scene``).
+"""
+import numpy as np
+
+from . import scene, synthetic
+
+
+class Workload:
+    """Arrays (float32, numpy) and camera parameters of one configuration."""
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def render_step(grid=(128, 128, 128), views=5, image=(256, 256), depth=128, max_u=2.0, yaw_span=120.0,
+                density_seed=0, velocity_seed=1, target_seed=2, blobs=6, target_noise=0.05):
+    """The differentiated single step (MacCormack advect, render, L2, backward):
+    grid ``D,H,W``, ``views`` cameras on a ``yaw_span`` arc about +y, frustum
+    ``depth x image``.  Blob centres span the middle 5/8 of each axis."""
+    D, H, W = grid
+    lo = np.array([W, H, D]) * 3 / 16
+    hi = np.array([W, H, D]) * 13 / 16
+    rho = synthetic.gaussian_blobs(grid, n=blobs, center_lo=lo, center_hi=hi, seed=density_seed)
+    rho_target = synthetic.gaussian_blobs(grid, n=blobs, center_lo=lo, center_hi=hi, seed=density_seed,
+                                          amp_noise=target_noise, noise_seed=target_seed)
+    ux, uy, uz = synthetic.curl_noise_mac(grid, max_u=max_u, seed=velocity_seed)
+    yaws = np.linspace(-yaw_span / 2, yaw_span / 2, views) if views > 1 else np.array([0.0])
+    cams = scene.orbit_cameras([depth, image[0], image[1]], list(yaws))
+    vol = scene.volume_transform(list(grid))
+    M = scene.model_params([vol])
+    V, P, F = scene.camera_params(cams)
+    return Workload(rho=rho, rho_target=rho_target, ux=ux, uy=uy, uz=uz, M=M, V=V, P=P, F=F, cameras=cams,
+                    image_dhw=(depth, image[0], image[1]), grid=tuple(grid), views=views,
+                    depth_step=cams[0].depth_step)
+
+
+def config2():
+    """128^3, 5 views at 256x256x128, max|u| = 2 cells/step."""
+    return render_step()
+
+
+def config1_small():
+    """64^3 grid, one camera 128x128x64, max|u| = 1 (the plain-forward case)."""
+    return render_step(grid=(64, 64, 64), views=1, image=(128, 128), depth=64, max_u=1.0)
+
+
+def algorithmic_bytes(grid, views, image, elem=4):
+    """Compulsory HBM bytes of one differentiated step: every tensor that must
+    cross HBM counted once at its storage size (density read / advected write /
+    read by render forward and backward / its gradient written and read / density
+    read and gradient written by the advection backward; velocity read forward
+    and backward and its gradient written; images written, read back and the
+    targets read).  Intermediates a fused implementation keeps on chip excluded."""
+    D, H, W = grid
+    n_rho = D * H * W
+    n_u = (W + 1) * H * D + W * (H + 1) * D + W * H * (D + 1)
+    px = views * image[0] * image[1]
+    return elem * (8 * n_rho + 3 * n_u) + 4 * 5 * px

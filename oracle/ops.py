@@ -176,7 +176,10 @@ def sample_grid_lut_grad(input, output_grad, lookup, interpolation=LINEAR, bound
                 if normalized_coords and grad_mode == "exact":
                     d, h, w = lut.shape[1:4]
                     lg = lg * np.array([w, h, d], dtype=dt)
-                glut[c, ..., :3] = lg
+                if grad_mode == "exact":
+                    glut[c, ..., :3] += lg  # every batch reading this lookup contributes
+                else:
+                    glut[c, ..., :3] = lg   # the reference kernel overwrites per batch
             if grad_mode == "reference":
                 scatter_linear_reference(gx[b], count, p, g, boundary)
             elif interpolation == LINEAR:

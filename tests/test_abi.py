@@ -1,0 +1,140 @@
+"""The C-ABI library: it loads, exports every function ``include/ngt_ops.h``
+declares, and its host-side validation rejects bad arguments with a status code
+and message before any device work (so these run without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import __graft_entry__
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    __graft_entry__.load_package()
+    from ngt_gb300 import _build, _lib
+    _build.build_library()
+    return _lib.load()
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "ngt_ops.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ngt_\w+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_binding_covers_header():
+    from ngt_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.SIGNATURES)
+
+
+def test_version(lib):
+    assert lib.ngt_version() >= 1
+
+
+def _lut_args(L, C=1, shape=(1, 4, 4, 4), lut=(1, 2, 2, 2, 4)):
+    a = L.SampleLutArgs()
+    a.dtype = L.F32
+    a.input_shape = L.I64x5(*shape, C)
+    a.lookup_shape = L.I64x5(*lut)
+    a.input = ctypes.c_void_p(0x1000)
+    a.lookup = ctypes.c_void_p(0x2000)
+    a.output = ctypes.c_void_p(0x3000)
+    a.interpolation, a.boundary = 1, 0
+    a.separate_camera_batch = 1
+    return a
+
+
+def test_rejects_three_channels(lib):
+    from ngt_gb300 import _lib as L
+    a = _lut_args(L, C=3)
+    assert lib.ngt_sample_lut_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"Channel" in lib.ngt_last_error_message()
+
+
+def test_rejects_bad_enums_and_shapes(lib):
+    from ngt_gb300 import _lib as L
+    a = _lut_args(L)
+    a.boundary = 7
+    assert lib.ngt_sample_lut_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    a = _lut_args(L, lut=(1, 2, 2, 2, 3))
+    assert lib.ngt_sample_lut_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    a = _lut_args(L)
+    a.input = None
+    assert lib.ngt_sample_lut_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    a = _lut_args(L)
+    a.normalized_coords, a.cell_center_offset = 1, 0.0
+    assert lib.ngt_sample_lut_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+
+
+def test_rejects_camera_batch_mismatch(lib):
+    from ngt_gb300 import _lib as L
+    a = _lut_args(L, shape=(2, 4, 4, 4), lut=(3, 2, 2, 2, 4))
+    a.separate_camera_batch = 0
+    assert lib.ngt_sample_lut_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"camera batch" in lib.ngt_last_error_message()
+
+
+def test_raymarch_validation(lib):
+    from ngt_gb300 import _lib as L
+    r = L.RaymarchArgs()
+    r.dtype = L.F32
+    r.input_shape = L.I64x5(1, 4, 4, 4, 2)
+    r.output_dhw = L.I64x3(4, 4, 4)
+    for f in ("input", "output", "matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(r, f, ctypes.c_void_p(0x1000))
+    r.num_cameras = 1
+    r.interpolation, r.boundary, r.blending_mode, r.separate_camera_batch = 1, 0, 0, 1
+    r.blending_mode = 1  # BEER_LAMBERT_EXCLUSIVE is not an op attribute value
+    assert lib.ngt_raymarch_fwd(ctypes.byref(r), None) == L.NGT_ERR_INVALID_ARGUMENT
+    r.blending_mode = 0
+    r.emission_channels = 2  # needs a one-channel input
+    assert lib.ngt_raymarch_fwd(ctypes.byref(r), None) == L.NGT_ERR_INVALID_ARGUMENT
+    g = L.RaymarchGradArgs()
+    g.fwd = r
+    g.fwd.emission_channels = 0
+    g.fwd.interpolation = 0  # gradients are LINEAR only
+    g.output_grad = g.input_grad = ctypes.c_void_p(0x1000)
+    assert lib.ngt_raymarch_bwd(ctypes.byref(g), None) == L.NGT_ERR_UNSUPPORTED
+
+
+def test_advect_validation(lib):
+    from ngt_gb300 import _lib as L
+    a = L.AdvectArgs()
+    a.dtype = L.F32
+    a.grid_dhw = L.I64x3(4, 4, 4)
+    a.channels = 1
+    for f in ("data", "vel_x", "vel_y", "vel_z", "output"):
+        setattr(a, f, ctypes.c_void_p(0x1000))
+    a.order, a.clamp, a.boundary = 2, 1, 1
+    assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT  # no fwd_field
+    a.order, a.clamp = 3, 0
+    assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    g = L.AdvectGradArgs()
+    g.fwd = a
+    g.fwd.order = 1
+    g.output_grad = g.data_grad = ctypes.c_void_p(0x1000)
+    assert lib.ngt_advect_maccormack_bwd(ctypes.byref(g), None) == L.NGT_ERR_WORKSPACE
+    assert lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g)) == 4 * 4 * 4 * 4 * 4
+
+
+def test_workspace_queries(lib):
+    from ngt_gb300 import _lib as L
+    g = L.SampleLutGradArgs()
+    g.fwd = _lut_args(L, shape=(2, 4, 5, 6))
+    g.grad_mode = 0
+    assert lib.ngt_sample_lut_bwd_workspace_bytes(ctypes.byref(g)) == 0
+    g.grad_mode = 1
+    assert lib.ngt_sample_lut_bwd_workspace_bytes(ctypes.byref(g)) == 2 * 4 * 5 * 6 * 4
+    shape = L.I64x5(1, 8, 8, 8, 2)
+    assert lib.ngt_mip_bytes(L.F32, shape, 2) == 4 * 4 * 4 * 2 * 4 + 256  # 512 B level 1, 64 B -> 256 level 2

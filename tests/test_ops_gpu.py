@@ -1,0 +1,301 @@
+"""GPU parity: every operator against the oracle on seeded inputs.
+
+Tolerances (float32, relative to the largest reference magnitude):
+* LUT resample forward and the MacCormack forward use the same operation order
+  as the oracle and must match bit for bit;
+* transform resample and raymarch forward: 2e-5 (positions come from fp32
+  matrix math on the GPU, fp64 in the oracle);
+* gradients: 1e-4 (atomic accumulation order), reference-normalised raymarch
+  gradient 5e-4 (division by summed sample weights).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import advect as oadvect
+from oracle import ops as oops
+
+pytestmark = pytest.mark.gpu
+
+
+def ngt():
+    import ngt_gb300.ops as ops
+    return ops
+
+
+def T(a, dtype=torch.float32):
+    return torch.as_tensor(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+
+
+def N(t):
+    return t.detach().cpu().numpy()
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.abs(a - b).max() / max(np.abs(a).max(), 1e-30)
+
+
+def scene_mats(vol_dhw=(8, 10, 12), cam_dhw=(8, 8, 6), yaws=(13, -47, 71)):
+    from ngt_gb300 import scene
+    vol = scene.volume_transform(list(vol_dhw))
+    cams = scene.orbit_cameras(list(cam_dhw), list(yaws))
+    M = scene.model_params([vol])
+    V, P, F = scene.camera_params(cams)
+    return M, V, P, F
+
+
+RNG = np.random.default_rng(7)
+
+# ---------------------------------------------------------------- LUT
+LUT_CASES = [(fm, bm, cn, sep, C) for fm in ("NEAREST", "LINEAR", "MIN", "MAX") for bm in ("BORDER", "CLAMP", "WRAP")
+             for cn in ("rel", "abs", "nrm") for sep in (True, False) for C in (1, 2, 4)]
+
+
+def lut_inputs(cn, C, seed=0):
+    r = np.random.default_rng(seed)
+    x = r.standard_normal((2, 5, 6, 7, C)).astype(np.float32)
+    lut = r.uniform(-1.5, 1.5, (2, 4, 5, 6, 4)).astype(np.float32)
+    lut[..., 3] = 0
+    if cn == "abs":
+        lut = lut + np.array([2, 2.5, 2, 0], np.float32)
+    if cn == "nrm":
+        lut = lut * np.float32(0.05)
+    kw = dict(relative_coords=cn != "abs", normalized_coords=cn == "nrm", cell_center_offset=0.5 if cn == "nrm" else 0.0)
+    return x, lut, kw
+
+
+@pytest.mark.parametrize("fm,bm,cn,sep,C", LUT_CASES)
+def test_lut_forward_bitexact(fm, bm, cn, sep, C):
+    x, lut, kw = lut_inputs(cn, C)
+    y = ngt().sample_grid_lut(T(x), T(lut), interpolation=fm, boundary=bm, separate_camera_batch=sep, **kw)
+    ref = oops.sample_grid_lut(x, lut, fm, bm, separate_camera_batch=sep, **kw)
+    assert y.shape == ref.shape
+    assert np.array_equal(N(y), ref)
+
+
+@pytest.mark.parametrize("mode", ["exact", "reference"])
+@pytest.mark.parametrize("fm,bm,cn,sep,C", [c for c in LUT_CASES if c[4] != 4])
+def test_lut_backward(fm, bm, cn, sep, C, mode):
+    x, lut, kw = lut_inputs(cn, C, seed=1)
+    gy = np.random.default_rng(2).standard_normal(oops.sample_grid_lut(x, lut, fm, bm, separate_camera_batch=sep,
+                                                                        **kw).shape).astype(np.float32)
+    gx, gl = ngt().sample_grid_lut_grad(T(x), T(gy), T(lut), interpolation=fm, boundary=bm,
+                                        separate_camera_batch=sep, grad_mode=mode, **kw)
+    rx, rl = oops.sample_grid_lut_grad(x, gy, lut, fm, bm, separate_camera_batch=sep, grad_mode=mode, **kw)
+    assert rel(rx, N(gx)) < 1e-5
+    if np.abs(rl).max() > 0:
+        assert rel(rl, N(gl)) < 1e-5
+    else:
+        assert np.abs(N(gl)).max() == 0
+
+
+@pytest.mark.parametrize("mipmode", ["NEAREST", "LINEAR"])
+def test_lut_mipmapped(mipmode):
+    x = RNG.standard_normal((1, 16, 12, 20, 2)).astype(np.float32)
+    lut = RNG.uniform(-3, 3, (2, 5, 6, 7, 4)).astype(np.float32)
+    lut[..., 3] = RNG.uniform(-0.5, 3.5, lut.shape[:-1])
+    kw = dict(interpolation="LINEAR", boundary="CLAMP", mipmapping=mipmode, num_mipmaps=2, mip_bias=0.25,
+              cell_center_offset=0.5)
+    y = ngt().sample_grid_lut(T(x), T(lut), **kw)
+    assert rel(oops.sample_grid_lut(x, lut, **kw), N(y)) < 1e-6
+
+
+def test_mip_pyramid():
+    from oracle import core
+    x = RNG.standard_normal((2, 9, 12, 16, 2)).astype(np.float32)
+    levels = ngt().mip_pyramid(T(x), 3)
+    for b in range(2):
+        ref = core.mip_pyramid(x[b], 3)
+        for lv in range(3):
+            assert np.array_equal(N(levels[lv][b]), ref[lv + 1])
+
+
+def test_lut_autograd_matches_grad_op():
+    x, lut, kw = lut_inputs("rel", 2, seed=3)
+    xt, lt = T(x).requires_grad_(), T(lut).requires_grad_()
+    y = ngt().sample_grid_lut(xt, lt, interpolation="LINEAR", boundary="CLAMP", **kw)
+    g = torch.randn_like(y)
+    y.backward(g)
+    gx, gl = ngt().sample_grid_lut_grad(T(x), g, T(lut), interpolation="LINEAR", boundary="CLAMP",
+                                        grad_mode="exact", **kw)
+    assert torch.equal(xt.grad, gx) or rel(N(gx), N(xt.grad)) < 1e-6
+    assert rel(N(gl), N(lt.grad)) < 1e-6
+
+
+# ---------------------------------------------------------- transform resample
+@pytest.mark.parametrize("cm", ["TRANSFORM_LINDEPTH", "TRANSFORM"])
+@pytest.mark.parametrize("fm", ["LINEAR", "NEAREST", "QUADRATIC"])
+@pytest.mark.parametrize("bm", ["BORDER", "CLAMP"])
+def test_transform(cm, fm, bm):
+    M, V, P, F = scene_mats()
+    x = RNG.uniform(0, 1, (1, 8, 10, 12, 2)).astype(np.float32)
+    y = ngt().sample_grid_transform(T(x), M, V, P, F, [8, 8, 6], fm, bm, coordinate_mode=cm)
+    ref = oops.sample_grid_transform(x, M, V, P, F, [8, 8, 6], fm, bm, coordinate_mode=cm)
+    if fm == "NEAREST":
+        assert np.isclose(N(y), ref, atol=1e-6).mean() > 0.99
+    else:
+        assert rel(ref, N(y)) < 2e-5
+    gy = RNG.standard_normal(ref.shape).astype(np.float32)
+    for mode in ("exact", "reference"):
+        if fm == "QUADRATIC" and bm == "BORDER" and mode == "reference":
+            continue
+        gx = ngt().sample_grid_transform_grad(T(x), T(gy), M, V, P, F, fm, bm, coordinate_mode=cm, grad_mode=mode)
+        rx = oops.sample_grid_transform_grad(x, gy, M, V, P, F, fm, bm, coordinate_mode=cm, grad_mode=mode)
+        if np.abs(rx).max() == 0:
+            assert np.abs(N(gx)).max() == 0
+        elif fm == "NEAREST":
+            assert np.isclose(N(gx), rx, atol=1e-4).mean() > 0.98
+        else:
+            assert rel(rx, N(gx)) < 1e-4
+
+
+@pytest.mark.parametrize("cm", ["TRANSFORM_LINDEPTH_REVERSE", "TRANSFORM_REVERSE"])
+def test_transform_reverse(cm):
+    M, V, P, F = scene_mats()
+    xf = RNG.uniform(0, 1, (1, 8, 8, 6, 1)).astype(np.float32)
+    y = ngt().sample_grid_transform(T(xf), M, V[:1], P[:1], F[:1], [8, 10, 12], "LINEAR", "BORDER",
+                                    coordinate_mode=cm)
+    ref = oops.sample_grid_transform(xf, M, V[:1], P[:1], F[:1], [8, 10, 12], "LINEAR", "BORDER", coordinate_mode=cm)
+    assert rel(ref, N(y)) < 2e-5
+
+
+def test_transform_mipmapped():
+    M, V, P, F = scene_mats(vol_dhw=(32, 32, 32), cam_dhw=(8, 8, 8))
+    x = RNG.uniform(0, 1, (1, 32, 32, 32, 1)).astype(np.float32)
+    kw = dict(interpolation="LINEAR", boundary="CLAMP", mipmapping="LINEAR", num_mipmaps=3)
+    y = ngt().sample_grid_transform(T(x), M, V, P, F, [8, 8, 8], **kw)
+    ref = oops.sample_grid_transform(x, M, V, P, F, [8, 8, 8], **kw)
+    assert rel(ref, N(y)) < 1e-4
+
+
+@pytest.mark.parametrize("lin", [True, False])
+def test_lod_transform(lin):
+    from ngt_gb300 import scene
+    vol = scene.volume_transform([8, 10, 12])
+    cams = scene.orbit_cameras([8, 8, 6], [13, -47])
+    MV = np.stack([scene.colmajor(c.view_matrix() @ vol.get_transform_matrix()) for c in cams])
+    _, P, F = scene.camera_params(cams)
+    y = ngt().lod_transform([8, 10, 12], MV, P, F, [8, 8, 6], linearize_depth=lin)
+    ref = oops.lod_transform([8, 10, 12], MV, P, F, [8, 8, 6], linearize_depth=lin)
+    assert rel(ref, N(y)) < 1e-5
+
+
+# -------------------------------------------------------------------- raymarch
+BLENDS = ["BEER_LAMBERT", "ALPHA", "ALPHA_ADDITIVE", "ADDITIVE"]
+
+
+@pytest.mark.parametrize("C", [1, 2, 4])
+@pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
+@pytest.mark.parametrize("blend", BLENDS)
+def test_raymarch(C, bm, blend):
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    x = (RNG.uniform(0, 1, (1, 10, 12, 14, C)) * 0.3).astype(np.float32)
+    y = ngt().raymarch_grid_transform(T(x), M, V, P, F, [10, 8, 6], "LINEAR", bm, blend)
+    ref = oops.raymarch_grid_transform(x, M, V, P, F, [10, 8, 6], "LINEAR", bm, blend)
+    assert rel(ref, N(y)) < 2e-5
+    gy = RNG.standard_normal(ref.shape).astype(np.float32)
+    gx = ngt().raymarch_grid_transform_grad(T(x), y, T(gy), M, V, P, F, [10, 8, 6], "LINEAR", bm, blend,
+                                            grad_mode="exact")
+    rx = oops.raymarch_grid_transform_grad(x, ref, gy, M, V, P, F, [10, 8, 6], "LINEAR", bm, blend, grad_mode="exact")
+    assert rel(rx, N(gx)) < 1e-4
+    gx = ngt().raymarch_grid_transform_grad(T(x), y, T(gy), M, V, P, F, [10, 8, 6], "LINEAR", bm, blend,
+                                            grad_mode="reference")
+    rx = oops.raymarch_grid_transform_grad(x, ref, gy, M, V, P, F, [10, 8, 6], "LINEAR", bm, blend,
+                                           grad_mode="reference")
+    assert rel(rx, N(gx)) < 5e-4
+
+
+def test_raymarch_nearest_and_batches():
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    M2 = np.concatenate([M, M])
+    x = (RNG.uniform(0, 1, (2, 10, 12, 14, 2)) * 0.3).astype(np.float32)
+    y = ngt().raymarch_grid_transform(T(x), M2, V, P, F, [10, 8, 6], "NEAREST", "BORDER", "BEER_LAMBERT")
+    ref = oops.raymarch_grid_transform(x, M2, V, P, F, [10, 8, 6], "NEAREST", "BORDER", "BEER_LAMBERT")
+    assert np.isclose(N(y), ref, rtol=1e-5, atol=1e-6).all(-1).mean() > 0.97
+    y = ngt().raymarch_grid_transform(T(x), M2, V[:2], P[:2], F[:2], [10, 8, 6], "LINEAR", "BORDER", "BEER_LAMBERT",
+                                      separate_camera_batch=False)
+    ref = oops.raymarch_grid_transform(x, M2, V[:2], P[:2], F[:2], [10, 8, 6], "LINEAR", "BORDER", "BEER_LAMBERT",
+                                       separate_camera_batch=False)
+    assert rel(ref, N(y)) < 2e-5
+
+
+@pytest.mark.parametrize("cb", [2, 4])
+def test_raymarch_emission_expansion(cb):
+    """A one-channel density with per-channel scales equals the materialised light grid."""
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    rho = (RNG.uniform(0, 1, (1, 10, 12, 14, 1)) * 0.3).astype(np.float32)
+    scale = [0.7, 1.3] if cb == 2 else [0.2, 0.5, 0.9, 1.3]
+    full = (rho * np.asarray(scale, np.float32)).astype(np.float32)
+    rt = T(rho).requires_grad_()
+    y = ngt().raymarch_grid_transform(rt, M, V, P, F, [10, 8, 6], emission_scale=scale)
+    ref = oops.raymarch_grid_transform(full, M, V, P, F, [10, 8, 6])
+    assert rel(ref, N(y)) < 2e-5
+    gy = RNG.standard_normal(ref.shape).astype(np.float32)
+    y.backward(T(gy))
+    gfull = oops.raymarch_grid_transform_grad(full, ref, gy, M, V, P, F, [10, 8, 6], grad_mode="exact")
+    assert rel((gfull * np.asarray(scale)).sum(-1, keepdims=True), N(rt.grad)) < 1e-4
+
+
+# ---------------------------------------------------------------- reduce blend
+@pytest.mark.parametrize("C", [1, 2, 4])
+@pytest.mark.parametrize("blend", BLENDS)
+@pytest.mark.parametrize("kd", [False, True])
+def test_reduce_blend(C, blend, kd):
+    x = RNG.uniform(0, 0.3, (2, 9, 5, 6, C)).astype(np.float32)
+    y = ngt().reduce_grid_blend(T(x), blend, kd)
+    ref = oops.reduce_grid_blend(x, blend, kd)
+    assert rel(ref, N(y)) < 1e-6
+    gy = RNG.standard_normal(ref.shape).astype(np.float32)
+    for mode in ("exact", "reference"):
+        gx = ngt().reduce_grid_blend_grad(T(gy), y, T(x), blend, kd, grad_mode=mode)
+        rx = oops.reduce_grid_blend_grad(gy, ref, x, blend, kd, grad_mode=mode)
+        assert rel(rx, N(gx)) < 1e-5
+
+
+# -------------------------------------------------------------------- advection
+def advect_inputs(shape=(10, 12, 14), max_u=2.0, seed=11, dtype=np.float32):
+    from ngt_gb300 import synthetic
+    rho = synthetic.gaussian_blobs(shape, n=4, sigma=(2, 4), seed=seed, dtype=dtype)
+    ux, uy, uz = synthetic.curl_noise_mac(shape, max_u=max_u, seed=seed + 1, smooth=2.0, dtype=dtype)
+    return rho, ux, uy, uz
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
+@pytest.mark.parametrize("order,clamp", [(2, "MC_SMOOTH"), (2, "NONE"), (1, "NONE"), (1, "NEGATIVE"), (2, "NEGATIVE")])
+def test_advect_forward_bitexact(bm, order, clamp):
+    from ngt_gb300 import advect
+    rho, ux, uy, uz = advect_inputs()
+    y = advect.warp(T(rho), T(ux), T(uy), T(uz), dt=1.0, order=order, clamp=clamp, boundary=bm)
+    ref = oadvect.density_maccormack(rho, ux, uy, uz, 1.0, order, clamp, bm)
+    assert np.array_equal(N(y), ref)
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER"])
+@pytest.mark.parametrize("mode", ["exact", "reference"])
+@pytest.mark.parametrize("order,clamp", [(2, "MC_SMOOTH"), (1, "NONE"), (2, "NEGATIVE")])
+def test_advect_backward(bm, mode, order, clamp):
+    from ngt_gb300 import advect, ops
+    rho, ux, uy, uz = advect_inputs(seed=13)
+    g = RNG.standard_normal(rho.shape).astype(np.float32)
+    ts = [T(a).requires_grad_() for a in (rho, ux, uy, uz)]
+    with ops.gradient_mode(mode):
+        y = advect.warp(*ts, dt=1.0, order=order, clamp=clamp, boundary=bm)
+        y.backward(T(g))
+    ref = oadvect.density_maccormack_grad(rho, ux, uy, uz, g, 1.0, order, clamp, bm, grad_mode=mode)
+    for t, r in zip(ts, ref):
+        assert rel(r, N(t.grad)) < 1e-4
+
+
+def test_advect_float64_matches_oracle():
+    from ngt_gb300 import advect
+    rho, ux, uy, uz = advect_inputs(dtype=np.float64)
+    g = RNG.standard_normal(rho.shape)
+    ts = [T(a, torch.float64).requires_grad_() for a in (rho, ux, uy, uz)]
+    y = advect.warp(*ts)
+    y.backward(T(g, torch.float64))
+    assert rel(oadvect.density_maccormack(rho, ux, uy, uz), N(y)) < 1e-13
+    ref = oadvect.density_maccormack_grad(rho, ux, uy, uz, g)
+    for t, r in zip(ts, ref):
+        assert rel(r, N(t.grad)) < 1e-11
