@@ -33,7 +33,7 @@ WORKLOAD = "MacCormack advect (MC_SMOOTH, CLAMP, dt=1) + 5-view Beer-Lambert ray
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--impl", default="ngt", choices=["ngt", "reference"])
@@ -85,12 +85,17 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < 10 and self.proc.poll() is None:
+            time.sleep(0.01)  # the first sample arrives before the timed region starts
+        self.skip = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -105,7 +110,7 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         rows = []
-        for ln in self.lines:
+        for ln in self.lines[getattr(self, "skip", 0):] or self.lines[-1:]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) >= 9:
                 rows.append(parts)
@@ -330,7 +335,7 @@ def kernel_stats(step, torch, dev, w, st, iters, flush):
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     calls = [("advect_fwd", lambda: step._call("ngt_advect_maccormack_fwd", ctypes.byref(step.adv), s)),
              ("raymarch_fwd", lambda: step._call("ngt_raymarch_fwd", ctypes.byref(step.ray), s)),
-             ("image_l2_loss", lambda: step._call("ngt_image_l2_loss", L.F32, step.pixels, 2, 1, _ptr(step.image),
+             ("image_l2_loss", lambda: step._call("ngt_image_l2_loss", L.F32 if st != torch.float64 else L.F64, step.pixels, 2, 1, _ptr(step.image),
                                                   _ptr(step.targets), _ptr(step.g_image), _ptr(step.loss), s)),
              ("raymarch_bwd", lambda: step._call("ngt_raymarch_bwd", ctypes.byref(step.ray_g), s)),
              ("advect_bwd", lambda: step._call("ngt_advect_maccormack_bwd", ctypes.byref(step.adv_g), s))]

@@ -95,7 +95,8 @@ typedef struct {
   void* input_grad;           /* shape of fwd.input */
   void* lookup_grad;          /* shape of fwd.lookup; may be null */
   int32_t grad_mode;          /* NGT_GRAD_EXACT / NGT_GRAD_REFERENCE */
-  void* workspace;            /* per-voxel sample counts (reference mode) */
+  int32_t deterministic;      /* exact LINEAR only: gather form, bit-reproducible input gradient */
+  void* workspace;            /* sample counts (reference mode) / gather buckets (deterministic) */
   size_t workspace_bytes;
 } ngt_sample_lut_grad_args;
 
@@ -263,6 +264,7 @@ typedef struct {
   void* vel_y_grad;
   void* vel_z_grad;
   int32_t grad_mode;
+  int32_t deterministic;      /* exact mode: gather form, bit-reproducible gradients */
   void* workspace;
   size_t workspace_bytes;
 } ngt_advect_grad_args;
@@ -271,15 +273,58 @@ int ngt_advect_maccormack_fwd(const ngt_advect_args* args, void* stream);
 int ngt_advect_maccormack_bwd(const ngt_advect_grad_args* args, void* stream);
 size_t ngt_advect_maccormack_bwd_workspace_bytes(const ngt_advect_grad_args* args);
 
+/* Self-advection of the MAC velocity: every face component is warped on its own
+ * staggered lattice by the velocity resampled onto that lattice (the other two
+ * components read at +-1/2 cell offsets).  Replaces VelocityGrid.warped
+ * (data_structures.py:1108-1164, with _sampled_to_component_shape :1655-1682 and
+ * _warp_vel_component :1081-1106): per component two resample_grid3D_offset
+ * calls (renderer.py:922-936) and four SampleGridLut calls.  The three warps all
+ * read the incoming velocity. */
+typedef struct {
+  int32_t dtype;              /* NGT_F32, NGT_F64, NGT_BF16, NGT_F16 */
+  int64_t grid_dhw[3];        /* cell grid D, H, W */
+  const void* vel_x;          /* D, H, W+1 */
+  const void* vel_y;          /* D, H+1, W */
+  const void* vel_z;          /* D+1, H, W */
+  float dt;
+  int32_t order;
+  int32_t clamp;
+  int32_t boundary;
+  void* out_x;                /* warped components, shapes as the inputs */
+  void* out_y;
+  void* out_z;
+  void* fwd_x;                /* per-component fwd fields (compute type), kept for the backward */
+  void* fwd_y;
+  void* fwd_z;
+} ngt_advect_velocity_args;
+
+typedef struct {
+  ngt_advect_velocity_args fwd;
+  const void* grad_x;         /* gradients of the warped components */
+  const void* grad_y;
+  const void* grad_z;
+  void* vel_x_grad;           /* gradients w.r.t. the incoming components */
+  void* vel_y_grad;
+  void* vel_z_grad;
+  int32_t grad_mode;
+  void* workspace;
+  size_t workspace_bytes;
+} ngt_advect_velocity_grad_args;
+
+int ngt_advect_velocity_fwd(const ngt_advect_velocity_args* args, void* stream);
+int ngt_advect_velocity_bwd(const ngt_advect_velocity_grad_args* args, void* stream);
+size_t ngt_advect_velocity_bwd_workspace_bytes(const ngt_advect_velocity_grad_args* args);
+
 /* ------------------------------------------------------------ step helpers */
 /* Image loss of the reconstruction step, 0.5 * sum over pixels of
  * (image[..., c] - target[..., c])^2 for the first ``loss_channels`` channels
  * (loss_dens_target, optimization.py:478, on the rendered light channel).
  * Writes the image gradient (zero in the remaining channels) and adds the loss
- * to *loss (device float; zero it first).  No reference counterpart as a
- * single call: the reference forms this loss with TensorFlow ops. */
+ * to *loss (device scalar of the image dtype, float or double; zero it first).
+ * No reference counterpart as a single call: the reference forms this loss
+ * with TensorFlow ops. */
 int ngt_image_l2_loss(int32_t dtype, int64_t pixels, int32_t channels, int32_t loss_channels, const void* image,
-                      const void* target, void* image_grad, float* loss, void* stream);
+                      const void* target, void* image_grad, void* loss, void* stream);
 
 /* ------------------------------------------------------------ diagnostics */
 const char* ngt_last_error_message(void);

@@ -34,7 +34,7 @@ class SampleLutArgs(ctypes.Structure):
 
 class SampleLutGradArgs(ctypes.Structure):
     _fields_ = [("fwd", SampleLutArgs), ("output_grad", c_vp), ("input_grad", c_vp), ("lookup_grad", c_vp),
-                ("grad_mode", c_i32), ("workspace", c_vp), ("workspace_bytes", c_sz)]
+                ("grad_mode", c_i32), ("deterministic", c_i32), ("workspace", c_vp), ("workspace_bytes", c_sz)]
 
 
 class SampleTransformArgs(ctypes.Structure):
@@ -88,8 +88,20 @@ class AdvectArgs(ctypes.Structure):
 
 class AdvectGradArgs(ctypes.Structure):
     _fields_ = [("fwd", AdvectArgs), ("output_grad", c_vp), ("data_grad", c_vp), ("vel_x_grad", c_vp),
-                ("vel_y_grad", c_vp), ("vel_z_grad", c_vp), ("grad_mode", c_i32), ("workspace", c_vp),
-                ("workspace_bytes", c_sz)]
+                ("vel_y_grad", c_vp), ("vel_z_grad", c_vp), ("grad_mode", c_i32), ("deterministic", c_i32),
+                ("workspace", c_vp), ("workspace_bytes", c_sz)]
+
+
+class AdvectVelocityArgs(ctypes.Structure):
+    _fields_ = [("dtype", c_i32), ("grid_dhw", I64x3), ("vel_x", c_vp), ("vel_y", c_vp), ("vel_z", c_vp),
+                ("dt", c_f32), ("order", c_i32), ("clamp", c_i32), ("boundary", c_i32), ("out_x", c_vp),
+                ("out_y", c_vp), ("out_z", c_vp), ("fwd_x", c_vp), ("fwd_y", c_vp), ("fwd_z", c_vp)]
+
+
+class AdvectVelocityGradArgs(ctypes.Structure):
+    _fields_ = [("fwd", AdvectVelocityArgs), ("grad_x", c_vp), ("grad_y", c_vp), ("grad_z", c_vp),
+                ("vel_x_grad", c_vp), ("vel_y_grad", c_vp), ("vel_z_grad", c_vp), ("grad_mode", c_i32),
+                ("workspace", c_vp), ("workspace_bytes", c_sz)]
 
 
 # name -> (argument types, result type)
@@ -113,6 +125,9 @@ SIGNATURES = {
     "ngt_advect_maccormack_fwd": ([ctypes.POINTER(AdvectArgs), c_vp], c_i32),
     "ngt_advect_maccormack_bwd": ([ctypes.POINTER(AdvectGradArgs), c_vp], c_i32),
     "ngt_advect_maccormack_bwd_workspace_bytes": ([ctypes.POINTER(AdvectGradArgs)], c_sz),
+    "ngt_advect_velocity_fwd": ([ctypes.POINTER(AdvectVelocityArgs), c_vp], c_i32),
+    "ngt_advect_velocity_bwd": ([ctypes.POINTER(AdvectVelocityGradArgs), c_vp], c_i32),
+    "ngt_advect_velocity_bwd_workspace_bytes": ([ctypes.POINTER(AdvectVelocityGradArgs)], c_sz),
     "ngt_image_l2_loss": ([c_i32, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp], c_i32),
     "ngt_last_error_message": ([], ctypes.c_char_p),
     "ngt_version": ([], c_i32),

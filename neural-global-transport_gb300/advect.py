@@ -10,7 +10,7 @@ import ctypes
 import torch
 
 from . import _lib as L
-from .ops import _code, _cuda, _ptr, _stream, _workspace, compute_dtype, get_gradient_mode
+from .ops import _code, _cuda, _ptr, _stream, _workspace, compute_dtype, get_deterministic, get_gradient_mode
 
 
 def _spatial(t, name):
@@ -64,7 +64,7 @@ def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary=
 
 
 def warp_backward(data, vx, vy, vz, fwd, grad, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP",
-                  grad_mode=None, velocity_grad=True):
+                  grad_mode=None, velocity_grad=True, deterministic=None):
     cd = compute_dtype(data)
     g = L.AdvectGradArgs()
     g.fwd = _args(data, vx, vy, vz, None, fwd, dt, order, clamp, boundary)
@@ -72,13 +72,13 @@ def warp_backward(data, vx, vy, vz, fwd, grad, dt=1.0, order=2, clamp="MC_SMOOTH
     gx = torch.empty(vx.shape, dtype=cd, device=data.device) if velocity_grad else None
     gy = torch.empty(vy.shape, dtype=cd, device=data.device) if velocity_grad else None
     gz = torch.empty(vz.shape, dtype=cd, device=data.device) if velocity_grad else None
-    g.output_grad, g.data_grad = _ptr(grad.to(cd).contiguous()), _ptr(gd)
+    keep = grad.to(cd).contiguous()
+    g.output_grad, g.data_grad = _ptr(keep), _ptr(gd)
     g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = _ptr(gx), _ptr(gy), _ptr(gz)
     g.grad_mode = L.GRAD[grad_mode or get_gradient_mode()]
+    g.deterministic = int(get_deterministic() if deterministic is None else deterministic)
     ws = _workspace(L.load().ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g)), data.device)
     g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
-    keep = grad.to(cd).contiguous()
-    g.output_grad = _ptr(keep)
     L.call("ngt_advect_maccormack_bwd", ctypes.byref(g), _stream())
     return gd, gx, gy, gz
 
@@ -88,15 +88,15 @@ class _Warp(torch.autograd.Function):
     def forward(ctx, data, vx, vy, vz, dt, order, clamp, boundary):
         out, fwd = warp_forward(data, vx, vy, vz, dt, order, clamp, boundary)
         ctx.save_for_backward(data, vx, vy, vz, fwd)
-        ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode())
+        ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode(), get_deterministic())
         return out
 
     @staticmethod
     def backward(ctx, grad):
         data, vx, vy, vz, fwd = ctx.saved_tensors
-        dt, order, clamp, boundary, mode = ctx.cfg
+        dt, order, clamp, boundary, mode, det = ctx.cfg
         gd, gx, gy, gz = warp_backward(data, vx, vy, vz, fwd, grad.contiguous(), dt, order, clamp, boundary, mode,
-                                       velocity_grad=any(ctx.needs_input_grad[1:4]))
+                                       velocity_grad=any(ctx.needs_input_grad[1:4]), deterministic=det)
         return gd, gx, gy, gz, None, None, None, None
 
 
@@ -115,3 +115,64 @@ def warp(data, vel_x, vel_y, vel_z, dt=1.0, order=2, clamp="MC_SMOOTH", boundary
     out = _Warp.apply(d, vx.to(d.dtype), vy.to(d.dtype), vz.to(d.dtype), float(dt), int(order), clamp.upper(),
                       boundary)
     return out[None] if lead else out
+
+
+# --------------------------------------------------------- velocity self-advection
+def _vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary):
+    a = L.AdvectVelocityArgs()
+    a.dtype = _code(vx)
+    D, H, W1 = vx.shape
+    a.grid_dhw = L.I64x3(D, H, W1 - 1)
+    a.vel_x, a.vel_y, a.vel_z = _ptr(vx), _ptr(vy), _ptr(vz)
+    a.dt, a.order, a.clamp, a.boundary = float(dt), int(order), L.CLAMP[clamp], L.BOUNDARY[boundary]
+    a.out_x, a.out_y, a.out_z = (_ptr(t) for t in outs)
+    a.fwd_x, a.fwd_y, a.fwd_z = (_ptr(t) for t in fwds)
+    return a
+
+
+class _WarpVelocity(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, vx, vy, vz, dt, order, clamp, boundary):
+        cd = compute_dtype(vx)
+        outs = [torch.empty_like(t) for t in (vx, vy, vz)]
+        fwds = [torch.empty(t.shape, dtype=cd, device=t.device) if order == 2 else None for t in (vx, vy, vz)]
+        L.call("ngt_advect_velocity_fwd", ctypes.byref(_vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary)),
+               _stream())
+        ctx.save_for_backward(vx, vy, vz, *[f for f in fwds if f is not None])
+        ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode())
+        return tuple(outs)
+
+    @staticmethod
+    def backward(ctx, gx, gy, gz):
+        saved = ctx.saved_tensors
+        vx, vy, vz = saved[:3]
+        fwds = list(saved[3:]) if len(saved) > 3 else [None, None, None]
+        dt, order, clamp, boundary, mode = ctx.cfg
+        cd = compute_dtype(vx)
+        gs = [(g if g is not None else torch.zeros(t.shape, device=t.device)).to(cd).contiguous()
+              for g, t in zip((gx, gy, gz), (vx, vy, vz))]
+        outs = [torch.empty(t.shape, dtype=cd, device=t.device) for t in (vx, vy, vz)]
+        g = L.AdvectVelocityGradArgs()
+        g.fwd = _vel_args(vx, vy, vz, (None, None, None), fwds, dt, order, clamp, boundary)
+        g.grad_x, g.grad_y, g.grad_z = (_ptr(t) for t in gs)
+        g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (_ptr(t) for t in outs)
+        g.grad_mode = L.GRAD[mode]
+        ws = _workspace(L.load().ngt_advect_velocity_bwd_workspace_bytes(ctypes.byref(g)), vx.device)
+        g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
+        L.call("ngt_advect_velocity_bwd", ctypes.byref(g), _stream())
+        return outs[0], outs[1], outs[2], None, None, None, None
+
+
+def warp_velocity(vel_x, vel_y, vel_z, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP"):
+    """Self-advection of a MAC velocity (``VelocityGrid.warped``): returns the
+    three warped face grids; differentiable w.r.t. all three inputs."""
+    lead = vel_x.dim() == 5
+    vx, vy, vz = _faces(vel_x, "vel_x"), _faces(vel_y, "vel_y"), _faces(vel_z, "vel_z")
+    D, H, W1 = vx.shape
+    if tuple(vy.shape) != (D, H + 1, W1 - 1) or tuple(vz.shape) != (D + 1, H, W1 - 1):
+        raise ValueError("shapes of components do not fit: x %s, y %s, z %s"
+                         % (tuple(vx.shape), tuple(vy.shape), tuple(vz.shape)))
+    if clamp.upper() == "MC":
+        raise NotImplementedError("MIM and MAX warp sampling have wrong gradients.")
+    out = _WarpVelocity.apply(vx, vy.to(vx.dtype), vz.to(vx.dtype), float(dt), int(order), clamp.upper(), boundary)
+    return tuple(o[None, ..., None] for o in out) if lead else out

@@ -1,26 +1,33 @@
-// Fused semi-Lagrangian / MacCormack advection of a cell-centred grid by a
-// MAC-staggered velocity, and its gradient.
+// Fused semi-Lagrangian / MacCormack advection by a MAC-staggered velocity and
+// its gradient: of a cell-centred grid (density) and of the velocity itself
+// (each face component on its own staggered lattice).
 //
-// The reference composes this in TensorFlow (VelocityGrid.warp,
-// data_structures.py:1690-1737): centred velocity (:1634-1654), lookup
+// The reference composes this in TensorFlow: VelocityGrid.warp
+// (data_structures.py:1690-1737) -- centred velocity (:1634-1654), lookup
 // ``-u*dt`` (:1684-1688), SampleGridLut forward and back, correction
-// ``fwd + 0.5*(data - back)``, MIN / MAX lookups and the MC_SMOOTH revert
-// clamp -- four resample launches and about six elementwise passes over HBM.
-// Here it is two kernels forward and three backward:
+// ``fwd + 0.5*(data - back)``, MIN / MAX lookups and the MC_SMOOTH revert clamp --
+// and VelocityGrid.warped (:1108-1164), which builds each component's lookup from
+// the other components resampled at +-1/2 cell offsets (:1655-1682) and warps it
+// the same way (_warp_vel_component, :1081-1106).  Here a warp is two kernels
+// forward and three backward:
 //
-//   forward 1: u_c from the faces, trilinear lookup  -> fwd field
-//   forward 2: back-trace of fwd, correction, extrema of the forward lookup's
-//              corners, revert clamp                    -> output
-//   backward 1: recompute state, route the gradient of the correction; scatter
-//               into the fwd-field gradient; lookup gradient of the back-trace
+//   forward 1: lookup from the velocity, trilinear forward trace -> fwd field
+//   forward 2: back-trace of fwd, correction, extrema of the forward trace's
+//              corners, revert clamp                                -> output
+//   backward 1: recompute the state, route the correction's gradient; scatter the
+//               back-trace adjoint into the fwd-field gradient; lookup gradient
+//               of the back-trace
 //   backward 2: scatter the fwd-field gradient into the data gradient; lookup
 //               gradient of the forward trace
-//   backward 3: centred-velocity gradient back to the faces (a gather, no atomics)
+//   backward 3: lookup gradient back to the faces (density: a gather over the two
+//               faces of each cell; velocity: the identity channel plus the
+//               adjoint of the +-1/2 offset resamples)
 //
-// Arithmetic of positions, interpolation and correction is explicitly rounded
-// in the composition's order, so float32 results equal an op-by-op evaluation
-// of the reference's formula and the clamp mask is reproduced exactly.
+// Arithmetic of positions, interpolation and correction is explicitly rounded in
+// the composition's order, so float32 results equal an op-by-op evaluation of
+// the reference's formula and the clamp mask is reproduced exactly.
 #include "ngt_common.cuh"
+#include "ngt_gather.cuh"
 #include "ngt_host.cuh"
 
 namespace ngt {
@@ -29,25 +36,89 @@ namespace {
 constexpr int kBlock = 256;
 
 template <class T>
-struct AdvParams {
-  const T* data;
+using CT = typename Compute<T>::type;
+
+// -------------------------------------------------------------- lookups
+// lookup = centred(u) * (-dt) (data_structures.py:1634-1654, 1684-1688)
+template <class T>
+struct CenteredLookup {
   const T* vx;
   const T* vy;
   const T* vz;
-  T* out;
-  typename Compute<T>::type* fwd;  // fwd field (compute type)
-  const typename Compute<T>::type* gout;
-  typename Compute<T>::type* gdata;
-  typename Compute<T>::type* gvx;
-  typename Compute<T>::type* gvy;
-  typename Compute<T>::type* gvz;
-  typename Compute<T>::type* gfwd;  // workspace: gradient w.r.t. the fwd field
-  typename Compute<T>::type* guc;   // workspace: gradient w.r.t. the centred velocity (3 per cell)
-  typename Compute<T>::type* buf;   // reference mode: unnormalised scatter
-  unsigned* cnt;                    // reference mode: sample counts
-  Dims d;
+  Dims d;  // cell lattice
   float dt;
+  __device__ __forceinline__ void operator()(int x, int y, int z, CT<T> lut[3]) const {
+    typedef CT<T> S;
+    const S h = S(0.5);
+    const S ux0 = S(ld(vx + (int64_t(z) * d.y + y) * (d.x + 1) + x));
+    const S ux1 = S(ld(vx + (int64_t(z) * d.y + y) * (d.x + 1) + x + 1));
+    const S uy0 = S(ld(vy + (int64_t(z) * (d.y + 1) + y) * d.x + x));
+    const S uy1 = S(ld(vy + (int64_t(z) * (d.y + 1) + y + 1) * d.x + x));
+    const S uz0 = S(ld(vz + (int64_t(z) * d.y + y) * d.x + x));
+    const S uz1 = S(ld(vz + (int64_t(z + 1) * d.y + y) * d.x + x));
+    const S ndt = S(-dt);
+    lut[0] = mul_rn(mul_rn(add_rn(ux1, ux0), h), ndt);
+    lut[1] = mul_rn(mul_rn(add_rn(uy1, uy0), h), ndt);
+    lut[2] = mul_rn(mul_rn(add_rn(uz1, uz0), h), ndt);
+  }
+};
+
+// Offset (added to the target index) at which component ``src`` is resampled on
+// the lattice of component ``tgt`` (data_structures.py:1655-1682).
+__device__ __forceinline__ float comp_offset(int src, int tgt, int axis) {
+  if (axis == src) return 0.5f;   // source faces sit half a cell below along their own axis
+  if (axis == tgt) return -0.5f;  // target faces sit half a cell below along theirs
+  return 0.0f;
+}
+
+__host__ __device__ __forceinline__ Dims face_dims(const Dims& c, int comp) {
+  return Dims{c.x + (comp == 0), c.y + (comp == 1), c.z + (comp == 2)};
+}
+
+// lookup of component ``tgt``: ``(-vel) * dt`` of all components on tgt's lattice
+template <class T>
+struct FaceLookup {
+  const T* u[3];
+  Dims cells;
+  int tgt;
+  int bm;
+  float dt;
+  __device__ __forceinline__ void operator()(int x, int y, int z, CT<T> lut[3]) const {
+    typedef CT<T> S;
+    const S ndt = S(dt);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      S v;
+      if (s == tgt) {
+        v = S(ld(u[s] + flat(x, y, z, face_dims(cells, s))));
+      } else {
+        S o[1];
+        read_linear<1>(u[s], add_rn(S(comp_offset(s, tgt, 0)), S(x)), add_rn(S(comp_offset(s, tgt, 1)), S(y)),
+                       add_rn(S(comp_offset(s, tgt, 2)), S(z)), face_dims(cells, s), bm, o);
+        v = o[0];
+      }
+      lut[s] = mul_rn(-v, ndt);
+    }
+  }
+};
+
+// ------------------------------------------------------------ MacCormack core
+template <class T>
+struct McParams {
+  const T* data;
+  T* out;
+  CT<T>* fwd;          // fwd field (compute type)
+  const CT<T>* gout;
+  CT<T>* gdata;
+  CT<T>* gfwd;         // workspace: gradient w.r.t. the fwd field
+  CT<T>* glut;         // workspace: gradient w.r.t. the lookup (3 per cell)
+  CT<T>* buf;          // reference mode: unnormalised scatter
+  unsigned* cnt;       // reference mode: sample counts
+  CT<T>* gback;        // deterministic mode: back-trace gradient per cell (gathered afterwards)
+  Dims d;
   int order, clamp, bm, reference;
+  int accumulate;      // add (atomically) the direct data gradient instead of writing it
+  int det;             // deterministic: no scatter here, the gather form follows
 };
 
 __device__ __forceinline__ void cell_of(int64_t i, const Dims& d, int& x, int& y, int& z) {
@@ -56,32 +127,15 @@ __device__ __forceinline__ void cell_of(int64_t i, const Dims& d, int& x, int& y
   z = int(i / (int64_t(d.x) * d.y));
 }
 
-// lookup = centred(u) * (-dt) (data_structures.py:1634-1654, 1684-1688)
-template <class T, class S>
-__device__ __forceinline__ void lookup(const AdvParams<T>& p, int x, int y, int z, S lut[3]) {
-  const Dims& d = p.d;
-  const S h = S(0.5);
-  const S ux0 = S(ld(p.vx + (int64_t(z) * d.y + y) * (d.x + 1) + x));
-  const S ux1 = S(ld(p.vx + (int64_t(z) * d.y + y) * (d.x + 1) + x + 1));
-  const S uy0 = S(ld(p.vy + (int64_t(z) * (d.y + 1) + y) * d.x + x));
-  const S uy1 = S(ld(p.vy + (int64_t(z) * (d.y + 1) + y + 1) * d.x + x));
-  const S uz0 = S(ld(p.vz + (int64_t(z) * d.y + y) * d.x + x));
-  const S uz1 = S(ld(p.vz + (int64_t(z + 1) * d.y + y) * d.x + x));
-  const S ndt = S(-p.dt);
-  lut[0] = mul_rn(mul_rn(add_rn(ux1, ux0), h), ndt);
-  lut[1] = mul_rn(mul_rn(add_rn(uy1, uy0), h), ndt);
-  lut[2] = mul_rn(mul_rn(add_rn(uz1, uz0), h), ndt);
-}
-
-template <int C, class T>
-__global__ void __launch_bounds__(kBlock) k_adv_fwd1(AdvParams<T> p) {
-  typedef typename Compute<T>::type S;
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_fwd1(McParams<T> p, LK lk) {
+  typedef CT<T> S;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= p.d.count()) return;
   int x, y, z;
   cell_of(i, p.d, x, y, z);
   S lut[3];
-  lookup<T, S>(p, x, y, z, lut);
+  lk(x, y, z, lut);
   S v[C];
   read_linear<C>(p.data, add_rn(lut[0], S(x)), add_rn(lut[1], S(y)), add_rn(lut[2], S(z)), p.d, p.bm, v);
   if (p.order == 1) {
@@ -96,7 +150,6 @@ __global__ void __launch_bounds__(kBlock) k_adv_fwd1(AdvParams<T> p) {
   }
 }
 
-// MacCormack state of one cell: fwd, back, correction, clamp mask and result
 template <int C, class S>
 struct McState {
   S fwd[C], back[C], corr[C], res[C];
@@ -104,7 +157,7 @@ struct McState {
 };
 
 template <int C, class T, class S>
-__device__ __forceinline__ void mc_state(const AdvParams<T>& p, int64_t i, int x, int y, int z, const S lut[3],
+__device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x, int y, int z, const S lut[3],
                                          McState<C, S>& s, S vb[8][C], Tri<S>& tb) {
   const S p2x = add_rn(-lut[0], S(x)), p2y = add_rn(-lut[1], S(y)), p2z = add_rn(-lut[2], S(z));
   tb = tri_setup(p2x, p2y, p2z, p.d, p.bm);
@@ -137,15 +190,15 @@ __device__ __forceinline__ void mc_state(const AdvParams<T>& p, int64_t i, int x
   }
 }
 
-template <int C, class T>
-__global__ void __launch_bounds__(kBlock) k_adv_fwd2(AdvParams<T> p) {
-  typedef typename Compute<T>::type S;
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_fwd2(McParams<T> p, LK lk) {
+  typedef CT<T> S;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= p.d.count()) return;
   int x, y, z;
   cell_of(i, p.d, x, y, z);
   S lut[3];
-  lookup<T, S>(p, x, y, z, lut);
+  lk(x, y, z, lut);
   McState<C, S> s;
   S vb[8][C];
   Tri<S> tb;
@@ -157,18 +210,24 @@ __global__ void __launch_bounds__(kBlock) k_adv_fwd2(AdvParams<T> p) {
   }
 }
 
+template <class S>
+__device__ __forceinline__ void put_direct(S* p, S v, int accumulate) {
+  if (accumulate) atomic_add(p, v);
+  else *p = v;
+}
+
 // backward 1: gradient of the correction; back-trace adjoint into gfwd
-template <int C, class T>
-__global__ void __launch_bounds__(kBlock) k_adv_bwd1(AdvParams<T> p) {
-  typedef typename Compute<T>::type S;
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
+  typedef CT<T> S;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= p.d.count()) return;
   int x, y, z;
   cell_of(i, p.d, x, y, z);
   S lut[3];
-  lookup<T, S>(p, x, y, z, lut);
+  lk(x, y, z, lut);
   S g[C];
-  S duc[3] = {S(0), S(0), S(0)};
+  S gl[3] = {S(0), S(0), S(0)};
   if (p.order == 1) {
     S v[C];
     if (p.clamp == NGT_CLAMP_NEGATIVE)
@@ -178,7 +237,7 @@ __global__ void __launch_bounds__(kBlock) k_adv_bwd1(AdvParams<T> p) {
       g[c] = p.gout[i * C + c];
       if (p.clamp == NGT_CLAMP_NEGATIVE && !(v[c] >= S(0))) g[c] = S(0);
       p.gfwd[i * C + c] = g[c];
-      p.gdata[i * C + c] = S(0);
+      if (!p.accumulate) p.gdata[i * C + c] = S(0);
     }
   } else {
     McState<C, S> s;
@@ -192,46 +251,75 @@ __global__ void __launch_bounds__(kBlock) k_adv_bwd1(AdvParams<T> p) {
       if (p.clamp == NGT_CLAMP_NEGATIVE && !(s.res[c] >= S(0))) g[c] = S(0);
       const S gc = s.mask[c] ? S(0) : g[c];
       gback[c] = -(S(0.5) * gc);
-      p.gdata[i * C + c] = S(0.5) * gc;  // direct term of the correction
+      put_direct(p.gdata + i * C + c, S(0.5) * gc, p.accumulate);  // direct term of the correction
     }
-    if (p.reference) {
+    const S p2x = add_rn(-lut[0], S(x)), p2y = add_rn(-lut[1], S(y)), p2z = add_rn(-lut[2], S(z));
+    if (p.det) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        p.gfwd[i * C + c] = g[c];
+        p.gback[i * C + c] = gback[c];
+      }
+    } else if (p.reference) {
 #pragma unroll
       for (int c = 0; c < C; ++c) p.gfwd[i * C + c] = g[c];
-      scatter_linear_counted<C>(p.buf, p.cnt, add_rn(-lut[0], S(x)), add_rn(-lut[1], S(y)), add_rn(-lut[2], S(z)),
-                                p.d, p.bm, gback);
+      scatter_linear_counted<C>(p.buf, p.cnt, p2x, p2y, p2z, p.d, p.bm, gback);
     } else {
 #pragma unroll
       for (int c = 0; c < C; ++c) atomic_add(p.gfwd + i * C + c, g[c]);
-      scatter_linear<C>(p.gfwd, add_rn(-lut[0], S(x)), add_rn(-lut[1], S(y)), add_rn(-lut[2], S(z)), p.d, p.bm,
-                        gback);
+      scatter_linear<C>(p.gfwd, p2x, p2y, p2z, p.d, p.bm, gback);
     }
     if (!(p.bm == BORDER && !tb.inside)) {
       S dx[C], dy[C], dz[C];
       tri_gradient<C>(vb, tb, dx, dy, dz);
-      // d pos2 / d u_c = +dt
+      // pos2 = idx - lut
 #pragma unroll
       for (int c = 0; c < C; ++c) {
-        duc[0] += S(p.dt) * gback[c] * dx[c];
-        duc[1] += S(p.dt) * gback[c] * dy[c];
-        duc[2] += S(p.dt) * gback[c] * dz[c];
+        gl[0] -= gback[c] * dx[c];
+        gl[1] -= gback[c] * dy[c];
+        gl[2] -= gback[c] * dz[c];
       }
     }
   }
-  p.guc[i * 3 + 0] = duc[0];
-  p.guc[i * 3 + 1] = duc[1];
-  p.guc[i * 3 + 2] = duc[2];
+  p.glut[i * 3 + 0] = gl[0];
+  p.glut[i * 3 + 1] = gl[1];
+  p.glut[i * 3 + 2] = gl[2];
 }
 
-// add normalised buffered scatter (reference mode) and clear the buffer
+// gather sources of the deterministic form: the back-trace (value gback at
+// idx - lut) and the forward trace (value gfwd at idx + lut)
+template <int C, class T, class LK>
+struct TraceSource {
+  const CT<T>* val;
+  LK lk;
+  Dims d;
+  int sign;  // +1 forward trace, -1 back-trace
+  __device__ __forceinline__ bool operator()(int64_t s, CT<T> pos[3], CT<T> g[C]) const {
+    typedef CT<T> S;
+    int x, y, z;
+    cell_of(s, d, x, y, z);
+    S lut[3];
+    lk(x, y, z, lut);
+    const S sg = S(sign);
+    pos[0] = add_rn(sg * lut[0], S(x));
+    pos[1] = add_rn(sg * lut[1], S(y));
+    pos[2] = add_rn(sg * lut[2], S(z));
+#pragma unroll
+    for (int c = 0; c < C; ++c) g[c] = val[s * C + c];
+    return true;
+  }
+};
+
+// add a normalised buffered scatter (reference mode) and clear the buffer
 template <int C, class S>
-__global__ void k_adv_norm(S* __restrict__ target, S* __restrict__ buf, unsigned* __restrict__ cnt, int64_t n) {
+__global__ void k_norm_add(S* __restrict__ target, S* __restrict__ buf, unsigned* __restrict__ cnt, int64_t n) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const unsigned k = cnt[i];
   if (k > 0) {
     const S w = S(1) / S(k);
 #pragma unroll
-    for (int c = 0; c < C; ++c) target[i * C + c] += buf[i * C + c] * w;
+    for (int c = 0; c < C; ++c) atomic_add(target + i * C + c, buf[i * C + c] * w);
   }
 #pragma unroll
   for (int c = 0; c < C; ++c) buf[i * C + c] = S(0);
@@ -239,173 +327,358 @@ __global__ void k_adv_norm(S* __restrict__ target, S* __restrict__ buf, unsigned
 }
 
 // backward 2: forward-trace adjoint into the data gradient
-template <int C, class T>
-__global__ void __launch_bounds__(kBlock) k_adv_bwd2(AdvParams<T> p) {
-  typedef typename Compute<T>::type S;
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
+  typedef CT<T> S;
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= p.d.count()) return;
   int x, y, z;
   cell_of(i, p.d, x, y, z);
   S lut[3];
-  lookup<T, S>(p, x, y, z, lut);
+  lk(x, y, z, lut);
   const S p1x = add_rn(lut[0], S(x)), p1y = add_rn(lut[1], S(y)), p1z = add_rn(lut[2], S(z));
   S g[C];
 #pragma unroll
   for (int c = 0; c < C; ++c) g[c] = p.gfwd[i * C + c];
-  if (p.reference) scatter_linear_counted<C>(p.buf, p.cnt, p1x, p1y, p1z, p.d, p.bm, g);
-  else scatter_linear<C>(p.gdata, p1x, p1y, p1z, p.d, p.bm, g);
+  if (p.det) {
+  } else if (p.reference) {
+    scatter_linear_counted<C>(p.buf, p.cnt, p1x, p1y, p1z, p.d, p.bm, g);
+  } else {
+    scatter_linear<C>(p.gdata, p1x, p1y, p1z, p.d, p.bm, g);
+  }
   const Tri<S> t = tri_setup(p1x, p1y, p1z, p.d, p.bm);
-  S duc[3] = {p.guc[i * 3 + 0], p.guc[i * 3 + 1], p.guc[i * 3 + 2]};
+  S gl[3] = {p.glut[i * 3 + 0], p.glut[i * 3 + 1], p.glut[i * 3 + 2]};
   if (!(p.bm == BORDER && !t.inside)) {
     S v[8][C], dx[C], dy[C], dz[C];
     tri_fetch<C>(p.data, t, p.d, v);
     tri_gradient<C>(v, t, dx, dy, dz);
-    // d pos1 / d u_c = -dt
+    // pos1 = idx + lut
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      duc[0] -= S(p.dt) * g[c] * dx[c];
-      duc[1] -= S(p.dt) * g[c] * dy[c];
-      duc[2] -= S(p.dt) * g[c] * dz[c];
+      gl[0] += g[c] * dx[c];
+      gl[1] += g[c] * dy[c];
+      gl[2] += g[c] * dz[c];
     }
   }
-  p.guc[i * 3 + 0] = duc[0];
-  p.guc[i * 3 + 1] = duc[1];
-  p.guc[i * 3 + 2] = duc[2];
+  p.glut[i * 3 + 0] = gl[0];
+  p.glut[i * 3 + 1] = gl[1];
+  p.glut[i * 3 + 2] = gl[2];
 }
 
-// backward 3: faces receive half of each adjacent cell's centred-velocity gradient
+// density backward 3: d u_c = -dt * d lut; each face receives half of its two cells
 template <class S>
-__global__ void __launch_bounds__(kBlock) k_adv_faces(const S* __restrict__ guc, S* __restrict__ gx, S* __restrict__ gy,
-                                                      S* __restrict__ gz, Dims d) {
+__global__ void __launch_bounds__(kBlock) k_centered_faces(const S* __restrict__ glut, S* __restrict__ gx,
+                                                           S* __restrict__ gy, S* __restrict__ gz, Dims d, float dt) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t nx = int64_t(d.x + 1) * d.y * d.z;
   const int64_t ny = int64_t(d.x) * (d.y + 1) * d.z;
   const int64_t nz = int64_t(d.x) * d.y * (d.z + 1);
-  const S h = S(0.5);
+  const S h = S(-0.5) * S(dt);
   if (i < nx) {
     const int x = int(i % (d.x + 1)), y = int((i / (d.x + 1)) % d.y), z = int(i / (int64_t(d.x + 1) * d.y));
     S s = S(0);
-    if (x > 0) s += guc[flat(x - 1, y, z, d) * 3 + 0] * h;
-    if (x < d.x) s += guc[flat(x, y, z, d) * 3 + 0] * h;
+    if (x > 0) s += glut[flat(x - 1, y, z, d) * 3 + 0] * h;
+    if (x < d.x) s += glut[flat(x, y, z, d) * 3 + 0] * h;
     gx[i] = s;
   } else if (i < nx + ny) {
     const int64_t j = i - nx;
     const int x = int(j % d.x), y = int((j / d.x) % (d.y + 1)), z = int(j / (int64_t(d.x) * (d.y + 1)));
     S s = S(0);
-    if (y > 0) s += guc[flat(x, y - 1, z, d) * 3 + 1] * h;
-    if (y < d.y) s += guc[flat(x, y, z, d) * 3 + 1] * h;
+    if (y > 0) s += glut[flat(x, y - 1, z, d) * 3 + 1] * h;
+    if (y < d.y) s += glut[flat(x, y, z, d) * 3 + 1] * h;
     gy[j] = s;
   } else if (i < nx + ny + nz) {
     const int64_t j = i - nx - ny;
     const int x = int(j % d.x), y = int((j / d.x) % d.y), z = int(j / (int64_t(d.x) * d.y));
     S s = S(0);
-    if (z > 0) s += guc[flat(x, y, z - 1, d) * 3 + 2] * h;
-    if (z < d.z) s += guc[flat(x, y, z, d) * 3 + 2] * h;
+    if (z > 0) s += glut[flat(x, y, z - 1, d) * 3 + 2] * h;
+    if (z < d.z) s += glut[flat(x, y, z, d) * 3 + 2] * h;
     gz[j] = s;
   }
 }
 
+// velocity backward 3 for component ``tgt``: the lookup channel of component s is
+// (-u_s resampled on tgt's lattice) * dt; its gradient goes to u_s directly
+// (s == tgt) or through the adjoint of the offset resample.
+template <class S>
+__global__ void __launch_bounds__(kBlock) k_face_lut_adjoint(const S* __restrict__ glut, S* gu0, S* gu1, S* gu2,
+                                                             Dims cells, int tgt, int bm, float dt, int reference,
+                                                             S* buf, unsigned* cnt) {
+  const Dims d = face_dims(cells, tgt);
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= d.count()) return;
+  int x, y, z;
+  cell_of(i, d, x, y, z);
+  S* gu[3] = {gu0, gu1, gu2};
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const S g = -(glut[i * 3 + s] * S(dt));
+    if (s == tgt) {
+      atomic_add(gu[s] + i, g);
+    } else {
+      const S gg[1] = {g};
+      const S px = add_rn(S(comp_offset(s, tgt, 0)), S(x)), py = add_rn(S(comp_offset(s, tgt, 1)), S(y)),
+              pz = add_rn(S(comp_offset(s, tgt, 2)), S(z));
+      if (reference) {
+        // one normalisation buffer per source component: buffers laid out back to back
+        int64_t off = 0;
+        for (int q = 0; q < s; ++q) off += face_dims(cells, q).count();
+        scatter_linear_counted<1>(buf + off, cnt + off, px, py, pz, face_dims(cells, s), bm, gg);
+      } else {
+        scatter_linear<1>(gu[s], px, py, pz, face_dims(cells, s), bm, gg);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host side
+size_t compute_size(int dtype) { return dtype == NGT_F64 ? 8 : 4; }
+
+int validate_common(int dtype, const int64_t* dhw, int order, int clamp, int boundary) {
+  if (!positive_shape(dhw, 3)) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: shapes must be positive");
+  if ((dhw[0] + 1) * (dhw[1] + 1) * (dhw[2] + 1) >= (int64_t(1) << 31))
+    return fail(NGT_ERR_INVALID_ARGUMENT, "advect: grid too large");
+  if (order != 1 && order != 2) return fail(NGT_ERR_INVALID_ARGUMENT, "Unsupported warp order '%d'", order);
+  if (clamp < NGT_CLAMP_NONE || clamp > NGT_CLAMP_NEGATIVE) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid clamp");
+  if (clamp == NGT_CLAMP_MC_SMOOTH && order != 2) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: MC_SMOOTH needs order 2");
+  if (boundary < NGT_BORDER || boundary > NGT_WRAP) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid boundary");
+  if (dtype < NGT_F32 || dtype > NGT_F16) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid dtype");
+  return NGT_OK;
+}
+
 int validate(const ngt_advect_args* a) {
   if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null arguments");
-  if (!positive_shape(a->grid_dhw, 3)) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: shapes must be positive");
+  int rc = validate_common(a->dtype, a->grid_dhw, a->order, a->clamp, a->boundary);
+  if (rc) return rc;
   if (!valid_channels(a->channels)) return fail(NGT_ERR_INVALID_ARGUMENT, "Only 1,2 and 4 Channel supported.");
-  if (a->grid_dhw[0] * a->grid_dhw[1] * a->grid_dhw[2] >= (int64_t(1) << 31))
-    return fail(NGT_ERR_INVALID_ARGUMENT, "advect: grid too large");
-  if (a->order != 1 && a->order != 2) return fail(NGT_ERR_INVALID_ARGUMENT, "Unsupported warp order '%d'", a->order);
-  if (a->clamp < NGT_CLAMP_NONE || a->clamp > NGT_CLAMP_NEGATIVE) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid clamp");
-  if (a->clamp == NGT_CLAMP_MC_SMOOTH && a->order != 2)
-    return fail(NGT_ERR_INVALID_ARGUMENT, "advect: MC_SMOOTH needs order 2");
-  if (a->boundary < NGT_BORDER || a->boundary > NGT_WRAP) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid boundary");
-  if (a->dtype < NGT_F32 || a->dtype > NGT_F16) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid dtype");
   if (!a->data || !a->vel_x || !a->vel_y || !a->vel_z) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null pointer");
   if (a->order == 2 && !a->fwd_field) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: MacCormack needs fwd_field");
   return NGT_OK;
 }
 
-size_t compute_size(int dtype) { return dtype == NGT_F64 ? 8 : 4; }
+Dims cells_of(const int64_t* dhw) { return Dims{int(dhw[2]), int(dhw[1]), int(dhw[0])}; }
+
+template <int C, class T, class LK>
+void launch_fwd(const McParams<T>& p, const LK& lk, cudaStream_t st) {
+  const unsigned nb = ceil_div_u(p.d.count(), kBlock);
+  k_mc_fwd1<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
+  if (p.order == 2) k_mc_fwd2<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
+}
+
+// bwd 1 + 2 of one warp; leaves the lookup gradient in p.glut
+template <int C, class T, class LK>
+int launch_bwd12(McParams<T>& p, const LK& lk, cudaStream_t st) {
+  typedef CT<T> S;
+  const int64_t n = p.d.count();
+  if (p.reference) {
+    if (cudaMemsetAsync(p.buf, 0, size_t(n) * C * sizeof(S), st) != cudaSuccess ||
+        cudaMemsetAsync(p.cnt, 0, size_t(n) * sizeof(unsigned), st) != cudaSuccess)
+      return check_launch("advect_bwd memset");
+  } else if (!p.det && cudaMemsetAsync(p.gfwd, 0, size_t(n) * C * sizeof(S), st) != cudaSuccess) {
+    return check_launch("advect_bwd memset");
+  }
+  const unsigned nb = ceil_div_u(n, kBlock);
+  k_mc_bwd1<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
+  if (p.det && p.order == 2)
+    gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st);
+  if (p.reference && p.order == 2) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gfwd, p.buf, p.cnt, n);
+  k_mc_bwd2<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
+  if (p.det) gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gfwd, lk, p.d, +1}, n, p.d, p.bm, p.cnt, p.gdata, 1, st);
+  if (p.reference) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gdata, p.buf, p.cnt, n);
+  return NGT_OK;
+}
 
 template <class T>
-AdvParams<T> params(const ngt_advect_args* a) {
-  typedef typename Compute<T>::type S;
-  AdvParams<T> p = {};
+McParams<T> density_params(const ngt_advect_args* a) {
+  McParams<T> p = {};
   p.data = static_cast<const T*>(a->data);
-  p.vx = static_cast<const T*>(a->vel_x);
-  p.vy = static_cast<const T*>(a->vel_y);
-  p.vz = static_cast<const T*>(a->vel_z);
   p.out = static_cast<T*>(a->output);
-  p.fwd = static_cast<S*>(a->fwd_field);
-  p.d = Dims{int(a->grid_dhw[2]), int(a->grid_dhw[1]), int(a->grid_dhw[0])};
-  p.dt = a->dt;
+  p.fwd = static_cast<CT<T>*>(a->fwd_field);
+  p.d = cells_of(a->grid_dhw);
   p.order = a->order;
   p.clamp = a->clamp;
   p.bm = a->boundary;
   return p;
 }
 
+template <class T>
+CenteredLookup<T> centered(const ngt_advect_args* a) {
+  return CenteredLookup<T>{static_cast<const T*>(a->vel_x), static_cast<const T*>(a->vel_y),
+                           static_cast<const T*>(a->vel_z), cells_of(a->grid_dhw), a->dt};
+}
+
 template <int C, class T>
-int fwd_typed(const ngt_advect_args* a, cudaStream_t st) {
-  AdvParams<T> p = params<T>(a);
-  const unsigned nb = ceil_div_u(p.d.count(), kBlock);
-  k_adv_fwd1<C, T><<<nb, kBlock, 0, st>>>(p);
-  if (p.order == 2) k_adv_fwd2<C, T><<<nb, kBlock, 0, st>>>(p);
+int density_fwd(const ngt_advect_args* a, cudaStream_t st) {
+  launch_fwd<C, T>(density_params<T>(a), centered<T>(a), st);
   return check_launch("ngt_advect_maccormack_fwd");
 }
 
 template <int C, class T>
-int bwd_typed(const ngt_advect_grad_args* g, cudaStream_t st) {
-  typedef typename Compute<T>::type S;
-  AdvParams<T> p = params<T>(&g->fwd);
+int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
+  typedef CT<T> S;
+  McParams<T> p = density_params<T>(&g->fwd);
   const int64_t n = p.d.count();
   p.gout = static_cast<const S*>(g->output_grad);
   p.gdata = static_cast<S*>(g->data_grad);
-  p.gvx = static_cast<S*>(g->vel_x_grad);
-  p.gvy = static_cast<S*>(g->vel_y_grad);
-  p.gvz = static_cast<S*>(g->vel_z_grad);
   p.reference = g->grad_mode == NGT_GRAD_REFERENCE;
+  p.det = !p.reference && g->deterministic;
   char* w = static_cast<char*>(g->workspace);
   p.gfwd = reinterpret_cast<S*>(w);
   w += size_t(n) * C * sizeof(S);
-  p.guc = reinterpret_cast<S*>(w);
+  p.glut = reinterpret_cast<S*>(w);
   w += size_t(n) * 3 * sizeof(S);
   if (p.reference) {
     p.buf = reinterpret_cast<S*>(w);
     w += size_t(n) * C * sizeof(S);
     p.cnt = reinterpret_cast<unsigned*>(w);
-    if (cudaMemsetAsync(p.buf, 0, size_t(n) * (C * sizeof(S) + sizeof(unsigned)), st) != cudaSuccess)
-      return check_launch("advect_bwd memset");
+  } else if (p.det) {
+    p.gback = reinterpret_cast<S*>(w);
+    w += size_t(n) * C * sizeof(S);
+    p.cnt = reinterpret_cast<unsigned*>(w);  // gather work area
   }
-  if (!p.reference && cudaMemsetAsync(p.gfwd, 0, size_t(n) * C * sizeof(S), st) != cudaSuccess)
-    return check_launch("advect_bwd memset");
-  const unsigned nb = ceil_div_u(n, kBlock);
-  k_adv_bwd1<C, T><<<nb, kBlock, 0, st>>>(p);
-  if (p.reference && p.order == 2) k_adv_norm<C, S><<<nb, kBlock, 0, st>>>(p.gfwd, p.buf, p.cnt, n);
-  k_adv_bwd2<C, T><<<nb, kBlock, 0, st>>>(p);
-  if (p.reference) k_adv_norm<C, S><<<nb, kBlock, 0, st>>>(p.gdata, p.buf, p.cnt, n);
-  if (p.gvx && p.gvy && p.gvz) {
-    const int64_t nf = int64_t(p.d.x + 1) * p.d.y * p.d.z + int64_t(p.d.x) * (p.d.y + 1) * p.d.z +
-                       int64_t(p.d.x) * p.d.y * (p.d.z + 1);
-    k_adv_faces<S><<<ceil_div_u(nf, kBlock), kBlock, 0, st>>>(p.guc, p.gvx, p.gvy, p.gvz, p.d);
+  int rc = launch_bwd12<C, T>(p, centered<T>(&g->fwd), st);
+  if (rc) return rc;
+  if (g->vel_x_grad && g->vel_y_grad && g->vel_z_grad) {
+    const Dims& d = p.d;
+    const int64_t nf = int64_t(d.x + 1) * d.y * d.z + int64_t(d.x) * (d.y + 1) * d.z + int64_t(d.x) * d.y * (d.z + 1);
+    k_centered_faces<S><<<ceil_div_u(nf, kBlock), kBlock, 0, st>>>(p.glut, static_cast<S*>(g->vel_x_grad),
+                                                                    static_cast<S*>(g->vel_y_grad),
+                                                                    static_cast<S*>(g->vel_z_grad), d, g->fwd.dt);
   }
   return check_launch("ngt_advect_maccormack_bwd");
 }
 
 template <class T>
-int fwd_c(const ngt_advect_args* a, cudaStream_t st) {
+int density_fwd_c(const ngt_advect_args* a, cudaStream_t st) {
   switch (a->channels) {
-    case 1: return fwd_typed<1, T>(a, st);
-    case 2: return fwd_typed<2, T>(a, st);
-    default: return fwd_typed<4, T>(a, st);
+    case 1: return density_fwd<1, T>(a, st);
+    case 2: return density_fwd<2, T>(a, st);
+    default: return density_fwd<4, T>(a, st);
   }
 }
 
 template <class T>
-int bwd_c(const ngt_advect_grad_args* g, cudaStream_t st) {
+int density_bwd_c(const ngt_advect_grad_args* g, cudaStream_t st) {
   switch (g->fwd.channels) {
-    case 1: return bwd_typed<1, T>(g, st);
-    case 2: return bwd_typed<2, T>(g, st);
-    default: return bwd_typed<4, T>(g, st);
+    case 1: return density_bwd<1, T>(g, st);
+    case 2: return density_bwd<2, T>(g, st);
+    default: return density_bwd<4, T>(g, st);
   }
 }
+
+// ----------------------------------------------------------- velocity warp
+int validate_vel(const ngt_advect_velocity_args* a) {
+  if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity: null arguments");
+  int rc = validate_common(a->dtype, a->grid_dhw, a->order, a->clamp, a->boundary);
+  if (rc) return rc;
+  if (!a->vel_x || !a->vel_y || !a->vel_z) return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity: null pointer");
+  if (a->order == 2 && (!a->fwd_x || !a->fwd_y || !a->fwd_z))
+    return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity: MacCormack needs the fwd fields");
+  return NGT_OK;
+}
+
+template <class T>
+FaceLookup<T> face_lookup(const ngt_advect_velocity_args* a, int tgt) {
+  FaceLookup<T> lk;
+  lk.u[0] = static_cast<const T*>(a->vel_x);
+  lk.u[1] = static_cast<const T*>(a->vel_y);
+  lk.u[2] = static_cast<const T*>(a->vel_z);
+  lk.cells = cells_of(a->grid_dhw);
+  lk.tgt = tgt;
+  lk.bm = a->boundary;
+  lk.dt = a->dt;
+  return lk;
+}
+
+template <class T>
+McParams<T> vel_params(const ngt_advect_velocity_args* a, int comp) {
+  const void* data[3] = {a->vel_x, a->vel_y, a->vel_z};
+  void* out[3] = {a->out_x, a->out_y, a->out_z};
+  void* fwd[3] = {a->fwd_x, a->fwd_y, a->fwd_z};
+  McParams<T> p = {};
+  p.data = static_cast<const T*>(data[comp]);
+  p.out = static_cast<T*>(out[comp]);
+  p.fwd = static_cast<CT<T>*>(fwd[comp]);
+  p.d = face_dims(cells_of(a->grid_dhw), comp);
+  p.order = a->order;
+  p.clamp = a->clamp;
+  p.bm = a->boundary;
+  return p;
+}
+
+template <class T>
+int vel_fwd(const ngt_advect_velocity_args* a, cudaStream_t st) {
+  for (int c = 0; c < 3; ++c) launch_fwd<1, T>(vel_params<T>(a, c), face_lookup<T>(a, c), st);
+  return check_launch("ngt_advect_velocity_fwd");
+}
+
+int64_t max_faces(const int64_t* dhw) {
+  const Dims c = cells_of(dhw);
+  int64_t m = 0;
+  for (int k = 0; k < 3; ++k) m = face_dims(c, k).count() > m ? face_dims(c, k).count() : m;
+  return m;
+}
+
+int64_t all_faces(const int64_t* dhw) {
+  const Dims c = cells_of(dhw);
+  return face_dims(c, 0).count() + face_dims(c, 1).count() + face_dims(c, 2).count();
+}
+
+template <class T>
+int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
+  typedef CT<T> S;
+  const ngt_advect_velocity_args* a = &g->fwd;
+  const Dims cells = cells_of(a->grid_dhw);
+  const int reference = g->grad_mode == NGT_GRAD_REFERENCE;
+  const int64_t nmax = max_faces(a->grid_dhw), nall = all_faces(a->grid_dhw);
+  char* w = static_cast<char*>(g->workspace);
+  S* gfwd = reinterpret_cast<S*>(w);
+  w += size_t(nmax) * sizeof(S);
+  S* glut = reinterpret_cast<S*>(w);
+  w += size_t(nmax) * 3 * sizeof(S);
+  S* buf = nullptr;
+  unsigned* cnt = nullptr;
+  if (reference) {
+    buf = reinterpret_cast<S*>(w);
+    w += size_t(nall) * sizeof(S);
+    cnt = reinterpret_cast<unsigned*>(w);
+  }
+  S* gu[3] = {static_cast<S*>(g->vel_x_grad), static_cast<S*>(g->vel_y_grad), static_cast<S*>(g->vel_z_grad)};
+  const void* go[3] = {g->grad_x, g->grad_y, g->grad_z};
+  for (int c = 0; c < 3; ++c)
+    if (cudaMemsetAsync(gu[c], 0, size_t(face_dims(cells, c).count()) * sizeof(S), st) != cudaSuccess)
+      return check_launch("advect_velocity_bwd memset");
+  for (int c = 0; c < 3; ++c) {
+    McParams<T> p = vel_params<T>(a, c);
+    p.gout = static_cast<const S*>(go[c]);
+    p.gdata = gu[c];
+    p.gfwd = gfwd;
+    p.glut = glut;
+    p.reference = reference;
+    p.buf = buf;
+    p.cnt = cnt;
+    p.accumulate = 1;
+    int rc = launch_bwd12<1, T>(p, face_lookup<T>(a, c), st);
+    if (rc) return rc;
+    if (reference && (cudaMemsetAsync(buf, 0, size_t(nall) * sizeof(S), st) != cudaSuccess ||
+                      cudaMemsetAsync(cnt, 0, size_t(nall) * sizeof(unsigned), st) != cudaSuccess))
+      return check_launch("advect_velocity_bwd memset");
+    k_face_lut_adjoint<S><<<ceil_div_u(p.d.count(), kBlock), kBlock, 0, st>>>(glut, gu[0], gu[1], gu[2], cells, c,
+                                                                               a->boundary, a->dt, reference, buf, cnt);
+    if (reference) {
+      int64_t off = 0;
+      for (int s = 0; s < 3; ++s) {
+        const int64_t ns = face_dims(cells, s).count();
+        if (s != c) k_norm_add<1, S><<<ceil_div_u(ns, kBlock), kBlock, 0, st>>>(gu[s], buf + off, cnt + off, ns);
+        off += ns;
+      }
+    }
+  }
+  return check_launch("ngt_advect_velocity_bwd");
+}
+
+template <class F>
+int by_dtype(int dtype, F&& f);
 
 }  // namespace
 }  // namespace ngt
@@ -418,10 +691,10 @@ extern "C" int ngt_advect_maccormack_fwd(const ngt_advect_args* a, void* stream)
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null output");
   cudaStream_t st = as_stream(stream);
   switch (a->dtype) {
-    case NGT_F32: return fwd_c<float>(a, st);
-    case NGT_F64: return fwd_c<double>(a, st);
-    case NGT_BF16: return fwd_c<__nv_bfloat16>(a, st);
-    default: return fwd_c<__half>(a, st);
+    case NGT_F32: return density_fwd_c<float>(a, st);
+    case NGT_F64: return density_fwd_c<double>(a, st);
+    case NGT_BF16: return density_fwd_c<__nv_bfloat16>(a, st);
+    default: return density_fwd_c<__half>(a, st);
   }
 }
 
@@ -432,6 +705,8 @@ extern "C" size_t ngt_advect_maccormack_bwd_workspace_bytes(const ngt_advect_gra
   const size_t cs = compute_size(g->fwd.dtype);
   size_t bytes = size_t(n) * size_t(C + 3) * cs;
   if (g->grad_mode == NGT_GRAD_REFERENCE) bytes += size_t(n) * (size_t(C) * cs + sizeof(unsigned));
+  else if (g->deterministic)
+    bytes += size_t(n) * size_t(C) * cs + gather_bytes(n, cells_of(g->fwd.grid_dhw), g->fwd.boundary) + 256;
   return bytes;
 }
 
@@ -447,9 +722,50 @@ extern "C" int ngt_advect_maccormack_bwd(const ngt_advect_grad_args* g, void* st
     return fail(NGT_ERR_WORKSPACE, "advect_bwd needs %zu workspace bytes", need);
   cudaStream_t st = as_stream(stream);
   switch (g->fwd.dtype) {
-    case NGT_F32: return bwd_c<float>(g, st);
-    case NGT_F64: return bwd_c<double>(g, st);
-    case NGT_BF16: return bwd_c<__nv_bfloat16>(g, st);
-    default: return bwd_c<__half>(g, st);
+    case NGT_F32: return density_bwd_c<float>(g, st);
+    case NGT_F64: return density_bwd_c<double>(g, st);
+    case NGT_BF16: return density_bwd_c<__nv_bfloat16>(g, st);
+    default: return density_bwd_c<__half>(g, st);
+  }
+}
+
+extern "C" int ngt_advect_velocity_fwd(const ngt_advect_velocity_args* a, void* stream) {
+  int rc = validate_vel(a);
+  if (rc) return rc;
+  if (!a->out_x || !a->out_y || !a->out_z) return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity: null output");
+  cudaStream_t st = as_stream(stream);
+  switch (a->dtype) {
+    case NGT_F32: return vel_fwd<float>(a, st);
+    case NGT_F64: return vel_fwd<double>(a, st);
+    case NGT_BF16: return vel_fwd<__nv_bfloat16>(a, st);
+    default: return vel_fwd<__half>(a, st);
+  }
+}
+
+extern "C" size_t ngt_advect_velocity_bwd_workspace_bytes(const ngt_advect_velocity_grad_args* g) {
+  if (!g) return 0;
+  const size_t cs = compute_size(g->fwd.dtype);
+  size_t bytes = size_t(max_faces(g->fwd.grid_dhw)) * 4 * cs;
+  if (g->grad_mode == NGT_GRAD_REFERENCE) bytes += size_t(all_faces(g->fwd.grid_dhw)) * (cs + sizeof(unsigned));
+  return bytes;
+}
+
+extern "C" int ngt_advect_velocity_bwd(const ngt_advect_velocity_grad_args* g, void* stream) {
+  if (!g) return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity_bwd: null arguments");
+  int rc = validate_vel(&g->fwd);
+  if (rc) return rc;
+  if (!g->grad_x || !g->grad_y || !g->grad_z || !g->vel_x_grad || !g->vel_y_grad || !g->vel_z_grad)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity_bwd: null pointer");
+  if (g->grad_mode != NGT_GRAD_EXACT && g->grad_mode != NGT_GRAD_REFERENCE)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity_bwd: invalid grad_mode");
+  const size_t need = ngt_advect_velocity_bwd_workspace_bytes(g);
+  if (!g->workspace || g->workspace_bytes < need)
+    return fail(NGT_ERR_WORKSPACE, "advect_velocity_bwd needs %zu workspace bytes", need);
+  cudaStream_t st = as_stream(stream);
+  switch (g->fwd.dtype) {
+    case NGT_F32: return vel_bwd<float>(g, st);
+    case NGT_F64: return vel_bwd<double>(g, st);
+    case NGT_BF16: return vel_bwd<__nv_bfloat16>(g, st);
+    default: return vel_bwd<__half>(g, st);
   }
 }

@@ -422,7 +422,7 @@ int validate(const ngt_raymarch_args* a, int& cin, int& cb) {
       return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: emission expansion needs a 1-channel input and 2 or 4 channels");
     cb = a->emission_channels;
   }
-  if (!a->input || !a->output || !a->matrix_m || !a->matrix_v || !a->matrix_p || !a->frustum)
+  if (!a->input || !a->matrix_m || !a->matrix_v || !a->matrix_p || !a->frustum)
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null pointer");
   if (a->num_cameras <= 0) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: num_cameras must be positive");
   if (!a->separate_camera_batch && a->num_cameras != a->input_shape[0])
@@ -510,6 +510,7 @@ extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
   int cin, cb;
   int rc = validate(a, cin, cb);
   if (rc) return rc;
+  if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null output");
   RayParams p = make_params(a);
   const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
   const int slots = num_slots(p);

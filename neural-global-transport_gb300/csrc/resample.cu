@@ -8,6 +8,7 @@
 // blockIdx.y enumerates (batch, camera) output slots, so all cameras of a batch
 // run in one launch with no per-camera host round trip.
 #include "ngt_common.cuh"
+#include "ngt_gather.cuh"
 #include "ngt_host.cuh"
 
 namespace ngt {
@@ -122,7 +123,7 @@ __global__ void __launch_bounds__(kBlock) k_lut_fwd(LutParams<T> p) {
 // One thread per (camera, output voxel); the batches reading that camera's
 // lookup are looped inside, so the lookup gradient is written once.
 template <int C, class T>
-__global__ void __launch_bounds__(kBlock) k_lut_bwd(LutParams<T> p, int reference) {
+__global__ void __launch_bounds__(kBlock) k_lut_bwd(LutParams<T> p, int reference, int skip_scatter) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t osz = p.dout.count();
   if (i >= osz) return;
@@ -164,7 +165,8 @@ __global__ void __launch_bounds__(kBlock) k_lut_bwd(LutParams<T> p, int referenc
         lg[2] += cur[2];
       }
     }
-    if (reference) {
+    if (skip_scatter) {
+    } else if (reference) {
       scatter_linear_counted<C>(ig, p.count + int64_t(b) * vsz, px, py, pz, p.din, p.bm, g);
     } else if (p.fm == LINEAR) {
       scatter_linear<C>(ig, px, py, pz, p.din, p.bm, g);
@@ -187,6 +189,28 @@ __global__ void __launch_bounds__(kBlock) k_lut_bwd(LutParams<T> p, int referenc
     o[3] = T(0);
   }
 }
+
+// Samples of batch b for the deterministic input gradient: every (camera, output
+// voxel) pair that reads batch b, at its lookup position.
+template <int C, class T>
+struct LutSource {
+  LutParams<T> p;
+  int b;
+  __device__ __forceinline__ bool operator()(int64_t s, T pos[3], T g[C]) const {
+    const int64_t osz = p.dout.count();
+    const int cam = p.sep ? int(s / osz) : b;
+    const int64_t i = p.sep ? s % osz : s;
+    const int slot = p.sep ? b * p.V + cam : b;
+    T x, y, z, w;
+    lut_position(p, cam, i, x, y, z, w);
+    pos[0] = sub_rn(x, p.cco);
+    pos[1] = sub_rn(y, p.cco);
+    pos[2] = sub_rn(z, p.cco);
+#pragma unroll
+    for (int c = 0; c < C; ++c) g[c] = p.out_grad[(int64_t(slot) * osz + i) * C + c];
+    return true;
+  }
+};
 
 // kNormalize3DGradients (resample_grid.cu.cc:1133-1151): divide by the per-voxel
 // sample count where it is non-zero.
@@ -500,6 +524,12 @@ int lut_fwd_typed(const ngt_sample_lut_args* a, cudaStream_t st) {
   return check_launch("ngt_sample_lut_fwd");
 }
 
+size_t lut_gather_bytes(const ngt_sample_lut_grad_args* a) {
+  const int64_t osz = a->fwd.lookup_shape[1] * a->fwd.lookup_shape[2] * a->fwd.lookup_shape[3];
+  const int64_t ns = (a->fwd.separate_camera_batch ? a->fwd.lookup_shape[0] : 1) * osz;
+  return gather_bytes(ns, dims_of(a->fwd.input_shape), a->fwd.boundary);
+}
+
 template <class T>
 int lut_bwd_typed(const ngt_sample_lut_grad_args* a, cudaStream_t st) {
   LutParams<T> p = lut_params<T>(&a->fwd);
@@ -519,10 +549,25 @@ int lut_bwd_typed(const ngt_sample_lut_grad_args* a, cudaStream_t st) {
     p.count = static_cast<unsigned*>(a->workspace);
     if (cudaMemsetAsync(p.count, 0, need, st) != cudaSuccess) return check_launch("sample_lut_bwd memset");
   }
+  const int det = !reference && a->deterministic;
+  if (det) {
+    const size_t need = lut_gather_bytes(a);
+    if (!a->workspace || a->workspace_bytes < need)
+      return fail(NGT_ERR_WORKSPACE, "sample_lut_bwd: deterministic mode needs %zu workspace bytes", need);
+  }
   const dim3 grid(ceil_div_u(p.dout.count(), kBlock), unsigned(p.V));
-  if (C == 1) k_lut_bwd<1, T><<<grid, kBlock, 0, st>>>(p, reference);
-  else if (C == 2) k_lut_bwd<2, T><<<grid, kBlock, 0, st>>>(p, reference);
-  else k_lut_bwd<4, T><<<grid, kBlock, 0, st>>>(p, reference);
+  if (C == 1) k_lut_bwd<1, T><<<grid, kBlock, 0, st>>>(p, reference, det);
+  else if (C == 2) k_lut_bwd<2, T><<<grid, kBlock, 0, st>>>(p, reference, det);
+  else k_lut_bwd<4, T><<<grid, kBlock, 0, st>>>(p, reference, det);
+  if (det) {
+    const int64_t ns = (p.sep ? int64_t(p.V) : 1) * p.dout.count();
+    for (int b = 0; b < p.N; ++b) {
+      T* ig = p.in_grad + int64_t(b) * vsz * C;
+      if (C == 1) gather_adjoint<1, T>(LutSource<1, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
+      else if (C == 2) gather_adjoint<2, T>(LutSource<2, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
+      else gather_adjoint<4, T>(LutSource<4, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
+    }
+  }
   if (reference) {
     const int64_t n = p.N * vsz;
     const unsigned nb = ceil_div_u(n, kBlock);
@@ -678,7 +723,9 @@ extern "C" int ngt_sample_lut_fwd(const ngt_sample_lut_args* a, void* stream) {
 }
 
 extern "C" size_t ngt_sample_lut_bwd_workspace_bytes(const ngt_sample_lut_grad_args* a) {
-  if (!a || a->grad_mode != NGT_GRAD_REFERENCE) return 0;
+  if (!a) return 0;
+  if (a->grad_mode == NGT_GRAD_EXACT && a->deterministic) return lut_gather_bytes(a);
+  if (a->grad_mode != NGT_GRAD_REFERENCE) return 0;
   const int64_t* s = a->fwd.input_shape;
   return size_t(s[0] * s[1] * s[2] * s[3]) * sizeof(unsigned);
 }
@@ -691,6 +738,8 @@ extern "C" int ngt_sample_lut_bwd(const ngt_sample_lut_grad_args* a, void* strea
   if (!a->output_grad || !a->input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "sample_lut_bwd: null pointer");
   if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "sample_lut_bwd: invalid grad_mode");
+  if (a->deterministic && a->grad_mode == NGT_GRAD_EXACT && a->fwd.interpolation != NGT_LINEAR)
+    return fail(NGT_ERR_UNSUPPORTED, "sample_lut_bwd: the deterministic gather form is for LINEAR interpolation");
   if (a->fwd.dtype == NGT_F64) return lut_bwd_typed<double>(a, as_stream(stream));
   return lut_bwd_typed<float>(a, as_stream(stream));
 }

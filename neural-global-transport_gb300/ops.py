@@ -21,6 +21,17 @@ import torch
 from . import _lib as L
 
 _GRAD_MODE = ["exact"]
+_DETERMINISTIC = [False]
+
+
+def set_deterministic(flag):
+    """Use the gather form (bit-reproducible) for the LUT-resample and advection
+    input gradients in exact mode."""
+    _DETERMINISTIC[0] = bool(flag)
+
+
+def get_deterministic():
+    return _DETERMINISTIC[0]
 
 
 def set_gradient_mode(mode):
@@ -129,13 +140,14 @@ def _lut_forward(input, lookup, a):
     return out
 
 
-def _lut_backward(input, output_grad, lookup, a, mode):
+def _lut_backward(input, output_grad, lookup, a, mode, deterministic=None):
     g = L.SampleLutGradArgs()
     g.fwd = _lut_args(input, lookup, None, a)
     input_grad = torch.empty_like(input)
     lookup_grad = torch.empty_like(lookup)
     g.output_grad, g.input_grad, g.lookup_grad = _ptr(output_grad), _ptr(input_grad), _ptr(lookup_grad)
     g.grad_mode = L.GRAD[mode]
+    g.deterministic = int(get_deterministic() if deterministic is None else deterministic)
     ws = _workspace(L.load().ngt_sample_lut_bwd_workspace_bytes(ctypes.byref(g)), input.device)
     g.workspace, g.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
     L.call("ngt_sample_lut_bwd", ctypes.byref(g), _stream())
@@ -147,13 +159,14 @@ class _SampleGridLut(torch.autograd.Function):
     def forward(ctx, input, lookup, attrs):
         ctx.attrs = attrs
         ctx.mode = get_gradient_mode()
+        ctx.det = get_deterministic()
         ctx.save_for_backward(input, lookup)
         return _lut_forward(input, lookup, attrs)
 
     @staticmethod
     def backward(ctx, grad):
         input, lookup = ctx.saved_tensors
-        gi, gl = _lut_backward(input, grad.contiguous(), lookup, ctx.attrs, ctx.mode)
+        gi, gl = _lut_backward(input, grad.contiguous(), lookup, ctx.attrs, ctx.mode, ctx.det)
         return gi, gl, None
 
 
@@ -175,7 +188,8 @@ def sample_grid_lut(input, lookup, interpolation="LINEAR", boundary="BORDER", mi
 
 def sample_grid_lut_grad(input, output_grad, lookup, interpolation="LINEAR", boundary="BORDER", mipmapping="NONE",
                          num_mipmaps=0, mip_bias=0.0, coordinate_mode="LOOKUP", cell_center_offset=0.0,
-                         separate_camera_batch=True, relative_coords=True, normalized_coords=False, grad_mode=None):
+                         separate_camera_batch=True, relative_coords=True, normalized_coords=False, grad_mode=None,
+                         deterministic=None):
     """``SampleGridLutGrad`` (resample_grid.cc:124-150): returns (input_grad, lookup_grad)."""
     input = _cuda(input, "input")
     attrs = dict(interpolation=interpolation, boundary=boundary, mipmapping=mipmapping, num_mipmaps=num_mipmaps,
@@ -183,7 +197,8 @@ def sample_grid_lut_grad(input, output_grad, lookup, interpolation="LINEAR", bou
                  separate_camera_batch=separate_camera_batch, relative_coords=relative_coords,
                  normalized_coords=normalized_coords)
     return _lut_backward(input, _cuda(output_grad, "output_grad").to(input.dtype),
-                         _cuda(lookup, "lookup").to(input.dtype), attrs, grad_mode or get_gradient_mode())
+                         _cuda(lookup, "lookup").to(input.dtype), attrs, grad_mode or get_gradient_mode(),
+                         deterministic)
 
 
 # ------------------------------------------------------------ transform resample

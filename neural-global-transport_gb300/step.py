@@ -34,7 +34,8 @@ class RenderAdvectStep:
         self.V = torch.as_tensor(V, dtype=torch.float32, device=dev).reshape(-1, 16).contiguous()
         self.P = torch.as_tensor(P, dtype=torch.float32, device=dev).reshape(-1, 16).contiguous()
         self.F = torch.as_tensor(F, dtype=torch.float32, device=dev).reshape(-1, 6).contiguous()
-        self.targets = targets.to(device=dev, dtype=torch.float32).contiguous()
+        self.targets = targets.to(device=dev, dtype=torch.float64 if rho.dtype == torch.float64
+                                  else torch.float32).contiguous()
         D, H, W = rho.shape[:3]
         nv = self.V.shape[0]
         dd, hh, ww = image_dhw
@@ -42,7 +43,7 @@ class RenderAdvectStep:
         depth_step = float(Fh[0, 1] - Fh[0, 0]) / dd
         self.emission = (light * depth_step, depth_step)
         st = rho.dtype
-        f32 = torch.float32
+        f32 = torch.float64 if st == torch.float64 else torch.float32  # compute / gradient precision
         self.rho_adv = torch.empty((D, H, W, 1), dtype=st, device=dev)
         self.fwd_field = torch.empty((D, H, W, 1), dtype=f32, device=dev)
         self.image = torch.empty((1, nv, hh, ww, 2), dtype=f32, device=dev)
@@ -112,10 +113,19 @@ class RenderAdvectStep:
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self.loss.zero_()
         self.forward(s.value)
-        self._call("ngt_image_l2_loss", L.F32, self.pixels, 2, 1, _ptr(self.image), _ptr(self.targets),
+        self._call("ngt_image_l2_loss", _code(self.image), self.pixels, 2, 1, _ptr(self.image), _ptr(self.targets),
                    _ptr(self.g_image), _ptr(self.loss), s)
         self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g), s)
         self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_g), s)
+
+    def loss_only(self):
+        """Forward and loss only (e.g. finite differences); returns the loss tensor."""
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self.loss.zero_()
+        self.forward(s.value)
+        self._call("ngt_image_l2_loss", _code(self.image), self.pixels, 2, 1, _ptr(self.image), _ptr(self.targets),
+                   _ptr(self.g_image), _ptr(self.loss), s)
+        return self.loss
 
     def capture(self):
         """Record one step as a CUDA graph (warm-up launch on a side stream first)."""

@@ -161,15 +161,22 @@ def resample_offset(src, target_shape, offset, boundary="CLAMP"):
     return core.read_linear(src[..., None], p, boundary)[..., 0]
 
 
-def resample_offset_adjoint(g, src_shape, offset, boundary="CLAMP"):
+def resample_offset_adjoint(g, src_shape, offset, boundary="CLAMP", grad_mode="exact"):
+    """Adjoint of :func:`resample_offset`; ``reference`` divides by the per-voxel
+    sample count as the LUT op's registered gradient does."""
     dt = g.dtype
     p = _idx(g.shape, dt) + np.asarray(offset, dt)
     out = np.zeros(tuple(src_shape) + (1,), dt)
-    ops.scatter_linear_exact(out, p, g[..., None], boundary)
+    if grad_mode == "exact":
+        ops.scatter_linear_exact(out, p, g[..., None], boundary)
+    else:
+        cnt = np.zeros(tuple(src_shape) + (1,), np.int64)
+        ops.scatter_linear_reference(out, cnt, p, g[..., None], boundary)
+        ops._normalize_by_count(out, cnt)
     return out[..., 0]
 
 
-def component_lut(comps, target, dt_step):
+def component_lut(comps, target, dt_step, boundary="CLAMP"):
     """Lookup for warping face component ``target`` ('x','y','z'):
     ``-vel*dt`` of all three components sampled on the target lattice
     (data_structures.py:1119,1127,1136)."""
@@ -177,7 +184,7 @@ def component_lut(comps, target, dt_step):
     shape = comps[names.index(target)].shape
     vel = []
     for n, c in zip(names, comps):
-        v = c if n == target else resample_offset(c, shape, COMPONENT_OFFSETS[(n, target)])
+        v = c if n == target else resample_offset(c, shape, COMPONENT_OFFSETS[(n, target)], boundary)
         vel.append((-v) * c.dtype.type(dt_step))
     return np.stack(vel, -1)
 
@@ -187,7 +194,7 @@ def velocity_maccormack(ux, uy, uz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary
     comps = (ux, uy, uz)
     out = []
     for n, c in zip(("x", "y", "z"), comps):
-        lut = component_lut(comps, n, dt)
+        lut = component_lut(comps, n, dt, boundary)
         out.append(maccormack(c[..., None], lut, order, clamp, boundary)[..., 0])
     return tuple(out)
 
@@ -200,7 +207,7 @@ def velocity_maccormack_grad(ux, uy, uz, grads, dt=1.0, order=2, clamp="MC_SMOOT
     names = ("x", "y", "z")
     acc = [np.zeros_like(c) for c in comps]
     for ti, (n, c) in enumerate(zip(names, comps)):
-        lut = component_lut(comps, n, dt)
+        lut = component_lut(comps, n, dt, boundary)
         g_data, g_lut = maccormack_grad(c[..., None], lut, grads[ti][..., None], order, clamp, boundary, grad_mode)
         acc[ti] += g_data[..., 0]
         g_vel = -(g_lut * c.dtype.type(dt))
@@ -208,5 +215,6 @@ def velocity_maccormack_grad(ux, uy, uz, grads, dt=1.0, order=2, clamp="MC_SMOOT
             if s == n:
                 acc[si] += g_vel[..., si]
             else:
-                acc[si] += resample_offset_adjoint(g_vel[..., si], comps[si].shape, COMPONENT_OFFSETS[(s, n)])
+                acc[si] += resample_offset_adjoint(g_vel[..., si], comps[si].shape, COMPONENT_OFFSETS[(s, n)],
+                                                   boundary, grad_mode)
     return tuple(acc)

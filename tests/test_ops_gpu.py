@@ -299,3 +299,69 @@ def test_advect_float64_matches_oracle():
     ref = oadvect.density_maccormack_grad(rho, ux, uy, uz, g)
     for t, r in zip(ts, ref):
         assert rel(r, N(t.grad)) < 1e-11
+
+
+# ------------------------------------------------------- velocity self-advection
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
+@pytest.mark.parametrize("order,clamp", [(2, "MC_SMOOTH"), (1, "NONE")])
+def test_velocity_advect_forward_bitexact(bm, order, clamp):
+    from ngt_gb300 import advect
+    _, ux, uy, uz = advect_inputs(shape=(9, 10, 11), seed=17)
+    out = advect.warp_velocity(T(ux), T(uy), T(uz), dt=1.0, order=order, clamp=clamp, boundary=bm)
+    ref = oadvect.velocity_maccormack(ux, uy, uz, 1.0, order, clamp, bm)
+    for o, r in zip(out, ref):
+        assert np.array_equal(N(o), r)
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER"])
+@pytest.mark.parametrize("mode", ["exact", "reference"])
+def test_velocity_advect_backward(bm, mode):
+    from ngt_gb300 import advect, ops
+    _, ux, uy, uz = advect_inputs(shape=(9, 10, 11), seed=19)
+    gs = [RNG.standard_normal(u.shape).astype(np.float32) for u in (ux, uy, uz)]
+    ts = [T(u).requires_grad_() for u in (ux, uy, uz)]
+    with ops.gradient_mode(mode):
+        out = advect.warp_velocity(*ts, boundary=bm)
+        torch.autograd.backward(out, [T(g) for g in gs])
+    ref = oadvect.velocity_maccormack_grad(ux, uy, uz, gs, boundary=bm, grad_mode=mode)
+    for t, r in zip(ts, ref):
+        assert rel(r, N(t.grad)) < 1e-4
+
+
+# ------------------------------------------------------------- deterministic mode
+@pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
+@pytest.mark.parametrize("sep", [True, False])
+def test_lut_backward_deterministic(bm, sep):
+    x, lut, kw = lut_inputs("rel", 2, seed=5)
+    lut = lut * np.float32(2.0)  # several samples per bucket
+    gy = RNG.standard_normal(oops.sample_grid_lut(x, lut, "LINEAR", bm, separate_camera_batch=sep,
+                                                  **kw).shape).astype(np.float32)
+    runs = [ngt().sample_grid_lut_grad(T(x), T(gy), T(lut), interpolation="LINEAR", boundary=bm,
+                                       separate_camera_batch=sep, grad_mode="exact", deterministic=True, **kw)
+            for _ in range(2)]
+    assert torch.equal(runs[0][0], runs[1][0]) and torch.equal(runs[0][1], runs[1][1])
+    rx, rl = oops.sample_grid_lut_grad(x, gy, lut, "LINEAR", bm, separate_camera_batch=sep, grad_mode="exact", **kw)
+    assert rel(rx, N(runs[0][0])) < 1e-5
+    assert rel(rl, N(runs[0][1])) < 1e-5
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
+def test_advect_backward_deterministic(bm):
+    from ngt_gb300 import advect, ops
+    rho, ux, uy, uz = advect_inputs(shape=(12, 14, 16), seed=23)
+    g = RNG.standard_normal(rho.shape).astype(np.float32)
+    grads = []
+    for _ in range(2):
+        ts = [T(a).requires_grad_() for a in (rho, ux, uy, uz)]
+        ops.set_deterministic(True)
+        try:
+            y = advect.warp(*ts, boundary=bm)
+            y.backward(T(g))
+        finally:
+            ops.set_deterministic(False)
+        grads.append([t.grad for t in ts])
+    for a, b in zip(*grads):
+        assert torch.equal(a, b)
+    ref = oadvect.density_maccormack_grad(rho, ux, uy, uz, g, boundary=bm)
+    for t, r in zip(grads[0], ref):
+        assert rel(r, N(t)) < 1e-4
