@@ -203,7 +203,9 @@ typedef struct {
   const void* output_grad;    /* same shape */
   void* input_grad;           /* shape of fwd.input (float32/64) */
   int32_t grad_mode;
-  void* workspace;            /* sample-weight sums (reference mode) */
+  void* workspace;            /* reference mode: gradient buffer + sample-weight sums;
+                                 exact Beer-Lambert: an extinction-sign flag
+                                 (size from ngt_raymarch_bwd_workspace_bytes) */
   size_t workspace_bytes;
 } ngt_raymarch_grad_args;
 

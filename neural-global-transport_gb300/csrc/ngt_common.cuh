@@ -493,65 +493,78 @@ __device__ __forceinline__ void scatter_quadratic_counted(S* __restrict__ grad, 
 // -------------------------------------------------------------- camera math
 // Matrices enter as 16 floats read column-major (transformations.hpp:42-47).
 // Per (batch, camera) the kernels need MV = V*M, its inverse and P, P^-1; they
-// are formed in double and rounded to float.
+// are formed in double and rounded to float (the reference inverts in float on
+// the host, transformations.hpp:48-68).
 struct Cam {
   float mv[16], mvi[16], p[16], pi[16];  // row-major: m[r*4+c]
   float near_, far_;
 };
 
-__device__ inline bool invert4(const double* a, double* inv) {
-  double m[4][8];
-  for (int r = 0; r < 4; ++r)
-    for (int c = 0; c < 8; ++c) m[r][c] = c < 4 ? a[r * 4 + c] : (c - 4 == r ? 1.0 : 0.0);
-  for (int col = 0; col < 4; ++col) {
-    int piv = col;
-    for (int r = col + 1; r < 4; ++r)
-      if (fabs(m[r][col]) > fabs(m[piv][col])) piv = r;
-    if (m[piv][col] == 0.0) return false;
-    if (piv != col)
-      for (int c = 0; c < 8; ++c) {
-        const double t = m[col][c];
-        m[col][c] = m[piv][c];
-        m[piv][c] = t;
-      }
-    const double s = 1.0 / m[col][col];
-    for (int c = 0; c < 8; ++c) m[col][c] *= s;
-    for (int r = 0; r < 4; ++r)
-      if (r != col) {
-        const double f = m[r][col];
-        for (int c = 0; c < 8; ++c) m[r][c] -= f * m[col][c];
-      }
-  }
-  for (int r = 0; r < 4; ++r)
-    for (int c = 0; c < 4; ++c) inv[r * 4 + c] = m[r][c + 4];
-  return true;
+// 3x3 determinant and signed 4x4 cofactor C_ij (row i, column j removed).
+__device__ __forceinline__ double det3(double a, double b, double c, double d, double e, double f, double g,
+                                       double h, double i) {
+  return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
 }
 
-// M16 may be null (identity model matrix).
-__device__ inline void build_cam(const float* M16, const float* V16, const float* P16, const float* F6, Cam& cam) {
-  double M[16], V[16], P[16], MV[16], inv[16];
+__device__ __forceinline__ double cofactor4(const double* m, int i, int j) {
+  double s[9];
+  int k = 0;
+#pragma unroll
   for (int r = 0; r < 4; ++r)
-    for (int c = 0; c < 4; ++c) {
-      M[r * 4 + c] = M16 ? (double)M16[c * 4 + r] : (r == c ? 1.0 : 0.0);
-      V[r * 4 + c] = (double)V16[c * 4 + r];
-      P[r * 4 + c] = (double)P16[c * 4 + r];
-    }
-  for (int r = 0; r < 4; ++r)
-    for (int c = 0; c < 4; ++c) {
-      double s = 0.0;
-      for (int k = 0; k < 4; ++k) s += V[r * 4 + k] * M[k * 4 + c];
-      MV[r * 4 + c] = s;
-    }
-  for (int i = 0; i < 16; ++i) {
-    cam.mv[i] = (float)MV[i];
-    cam.p[i] = (float)P[i];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      if (r != i && c != j) s[k++] = m[r * 4 + c];
+  const double d = det3(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8]);
+  return ((i + j) & 1) ? -d : d;
+}
+
+// Element (r, c) of the inverse by the adjugate: C_cr / det, det expanded along row 0.
+__device__ __forceinline__ double inverse_element(const double* m, int r, int c) {
+  double det = 0.0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) det += m[j] * cofactor4(m, 0, j);
+  return cofactor4(m, c, r) / det;
+}
+
+// Scratch of build_cam_warp: M, V, P, MV in double (row-major).
+struct CamScratch {
+  double M[16], V[16], P[16], MV[16];
+};
+
+// Forms ``cam`` cooperatively with the 32 lanes of the calling warp (every lane
+// must call it): lanes 0-15 one element each of MV = V*M and of MV^-1, lanes
+// 16-31 one element each of P^-1, all in double and rounded to float.  M16 may
+// be null (identity model matrix).  Inputs are column-major (as the reference's
+// setTransformations reads them); Cam holds row-major matrices.
+__device__ inline void build_cam_warp(const float* M16, const float* V16, const float* P16, const float* F6,
+                                      Cam& cam, CamScratch& sh) {
+  const int lane = threadIdx.x & 31;
+  const int e = lane & 15, r = e >> 2, c = e & 3;
+  if (lane < 16) {
+    sh.M[e] = M16 ? (double)M16[c * 4 + r] : (r == c ? 1.0 : 0.0);
+    sh.V[e] = (double)V16[c * 4 + r];
+  } else {
+    sh.P[e] = (double)P16[c * 4 + r];
   }
-  invert4(MV, inv);
-  for (int i = 0; i < 16; ++i) cam.mvi[i] = (float)inv[i];
-  invert4(P, inv);
-  for (int i = 0; i < 16; ++i) cam.pi[i] = (float)inv[i];
-  cam.near_ = F6[0];
-  cam.far_ = F6[1];
+  __syncwarp();
+  if (lane < 16) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s += sh.V[r * 4 + k] * sh.M[k * 4 + c];
+    sh.MV[e] = s;
+    cam.mv[e] = (float)s;
+  } else {
+    cam.p[e] = (float)sh.P[e];
+  }
+  __syncwarp();
+  if (lane < 16)
+    cam.mvi[e] = (float)inverse_element(sh.MV, r, c);
+  else
+    cam.pi[e] = (float)inverse_element(sh.P, r, c);
+  if (lane == 0) {
+    cam.near_ = F6[0];
+    cam.far_ = F6[1];
+  }
 }
 
 __device__ __forceinline__ void mat4_apply(const float* m, const float v[4], float o[4]) {

@@ -39,6 +39,7 @@ struct RayParams {
   int fm, bm, blend;
   float scale[4];
   int slot0;             // first (batch, camera) slot of this launch
+  const int* flag;       // exact Beer-Lambert backward: nonzero if an extinction sample can be negative
 };
 
 __device__ __forceinline__ void slot_to_bc(const RayParams& p, int slot, int& b, int& c, int& oslot) {
@@ -164,17 +165,19 @@ __device__ __forceinline__ void scatter_cell(const RayParams& p, S* __restrict__
   }
 }
 
-__device__ __forceinline__ void load_cam(const RayParams& p, int b, int c, Cam& cam) {
-  build_cam(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam);
+// The block's camera, formed by warp 0; the caller synchronises the block.
+__device__ __forceinline__ void load_cam(const RayParams& p, int b, int c, Cam& cam, CamScratch& sh) {
+  if (threadIdx.x < 32) build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, sh);
 }
 
 // ----------------------------------------------------------------- forward
 template <int CIN, int CB, class T, class S>
 __global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
   __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  if (threadIdx.x == 0) load_cam(p, b, c, cam);
+  load_cam(p, b, c, cam, cam_sh);
   __syncthreads();
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
   int px, py;
@@ -209,9 +212,10 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
 template <int CIN, int CB, class T, class S>
 __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
   __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  if (threadIdx.x == 0) load_cam(p, b, c, cam);
+  load_cam(p, b, c, cam, cam_sh);
   __syncthreads();
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
   int px, py;
@@ -223,6 +227,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
   S* grad = reinterpret_cast<S*>(p.in_grad) + int64_t(b) * p.din.count() * CIN;
   const Ray r = ray_setup(cam, px, py, p);
   if (!r.hit || r.steps <= 0) return;
+  if (p.flag && *p.flag == 0) return;  // Beer-Lambert with non-negative extinction: k_raymarch_bwd_bl
   S G[CB];
   const S* og = reinterpret_cast<const S*>(p.out_grad) + ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
 #pragma unroll
@@ -303,6 +308,79 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
   }
 }
 
+// ------------------------------------ exact Beer-Lambert backward, one pass
+// With every extinction sample sigma_k >= 0 the density never reaches the
+// max(d + sigma, 0) clamp, and the adjoint of the front-to-back blend
+//   d_k = d_{k-1} + sigma_k,  t_k = exp(-d_k),  L_c += t_k * l_kc
+// is, in forward order,
+//   dl_kc     = t_k * gL_c
+//   dsigma_k  = gD - sum_{j>=k} t_j (l_j . gL) = gD - (L . gL - W_{k-1}),
+// W_{k-1} = sum_{j<k} t_j (l_j . gL) accumulated on the way and L the forward
+// output.  One march replaces the checkpointed recomputation; the sign of the
+// extinction channel is checked over the whole grid first (k_extinction_sign),
+// and a launch that can see a negative sample runs k_raymarch_bwd_exact.
+template <int CIN, int CB, class T, class S>
+__global__ void __launch_bounds__(kThreads) k_raymarch_bwd_bl(RayParams p) {
+  if (*p.flag != 0) return;
+  __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
+  int b, c, oslot;
+  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
+  load_cam(p, b, c, cam, cam_sh);
+  __syncthreads();
+  const int tiles_x = (p.W + kTileX - 1) / kTileX;
+  int px, py;
+  pixel_of_thread(px, py);
+  px += (blockIdx.x % tiles_x) * kTileX;
+  py += (blockIdx.x / tiles_x) * kTileY;
+  if (px >= p.W || py >= p.H) return;
+  const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  S* grad = reinterpret_cast<S*>(p.in_grad) + int64_t(b) * p.din.count() * CIN;
+  const Ray r = ray_setup(cam, px, py, p);
+  if (!r.hit || r.steps <= 0) return;
+  const int64_t o = ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
+  S G[CB];
+  S lgf = S(0);
+#pragma unroll
+  for (int k = 0; k < CB; ++k) G[k] = reinterpret_cast<const S*>(p.out_grad)[o + k];
+#pragma unroll
+  for (int k = 0; k < CB - 1; ++k) lgf += G[k] * reinterpret_cast<const S*>(p.out_fwd)[o + k];
+  const S gD = G[CB - 1];
+  S d = S(0), w = S(0);
+  float pos[3] = {r.s[0], r.s[1], r.s[2]};
+  for (int i = 0; i < r.steps; ++i) {
+    S cell[CB], dcell[CB];
+    sample_cell<CIN, CB>(g, pos, p, cell);
+    d = d + cell[CB - 1];
+    const S t = ex(-d);
+    S lg = S(0);
+#pragma unroll
+    for (int k = 0; k < CB - 1; ++k) {
+      lg += cell[k] * G[k];
+      dcell[k] = t * G[k];
+    }
+    dcell[CB - 1] = gD - (lgf - w);
+    w += t * lg;
+    scatter_cell<CIN, CB>(p, grad, pos, dcell);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
+  }
+}
+
+// Sets *flag when some voxel makes a negative extinction sample possible: a
+// negative extinction channel (CIN == CB), or a one-channel density whose sign
+// is opposite to the extinction scale.  Linear interpolation of non-negative
+// values (border cells read as 0) is non-negative.
+template <int CIN, int CB, class T>
+__global__ void k_extinction_sign(const T* __restrict__ g, int64_t nvox, float sscale, int* flag) {
+  int neg = 0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nvox; i += int64_t(gridDim.x) * blockDim.x) {
+    const float v = float(ld(g + i * CIN + (CIN - 1)));
+    neg |= (CIN == CB) ? (v < 0.0f) : (sscale * v < 0.0f);
+  }
+  if (__syncthreads_or(neg) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 // --------------------------------------------------- reference backward
 // scatterGrad3DInterpolated with per-voxel weight sums (sampling_v2.hpp:438-559)
 template <int C, class S>
@@ -348,9 +426,10 @@ __device__ __forceinline__ void scatter_weighted(S* __restrict__ buf, S* __restr
 template <int CIN, int CB, class T, class S>
 __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_reference(RayParams p) {
   __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  if (threadIdx.x == 0) load_cam(p, b, c, cam);
+  load_cam(p, b, c, cam, cam_sh);
   __syncthreads();
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
   int px, py;
@@ -466,16 +545,25 @@ int num_slots(const RayParams& p) { return p.sep ? p.N * p.ncam : p.N; }
 template <template <int, int, class, class> class K, class T, class S>
 int dispatch_channels(int cin, int cb, dim3 grid, cudaStream_t st, const RayParams& p);
 
-enum Which { FWD = 0, BWD_EXACT = 1, BWD_REF = 2 };
+enum Which { FWD = 0, BWD_EXACT = 1, BWD_REF = 2, BWD_BL = 3, SIGN = 4 };
 
 template <int CIN, int CB, class T, class S>
 void launch(int which, dim3 grid, cudaStream_t st, const RayParams& p) {
-  if (which == FWD)
+  if (which == FWD) {
     k_raymarch_fwd<CIN, CB, T, S><<<grid, kThreads, 0, st>>>(p);
-  else if (which == BWD_EXACT)
+  } else if (which == BWD_EXACT) {
     k_raymarch_bwd_exact<CIN, CB, T, S><<<grid, kThreads, 0, st>>>(p);
-  else
+  } else if (which == BWD_BL) {
+    if (CB > 1) k_raymarch_bwd_bl<CIN, CB, T, S><<<grid, kThreads, 0, st>>>(p);
+  } else if (which == SIGN) {
+    const int64_t nvox = int64_t(p.N) * p.din.count();
+    const int64_t nb = (nvox + 255) / 256;
+    const unsigned blocks = unsigned(nb < 152 * 8 ? nb : 152 * 8);
+    k_extinction_sign<CIN, CB, T><<<blocks, 256, 0, st>>>(static_cast<const T*>(p.input), nvox,
+                                                         p.scale[CB - 1], const_cast<int*>(p.flag));
+  } else {
     k_raymarch_bwd_reference<CIN, CB, T, S><<<grid, kThreads, 0, st>>>(p);
+  }
 }
 
 template <class T, class S>
@@ -523,8 +611,16 @@ extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
   return check_launch("ngt_raymarch_fwd");
 }
 
+// Exact Beer-Lambert backward: one int flag; reference: gradient buffer + weight sums.
+bool needs_sign_flag(const ngt_raymarch_grad_args* a) {
+  const int cin = int(a->fwd.input_shape[4]);
+  const int cb = a->fwd.emission_channels ? a->fwd.emission_channels : cin;
+  return a->grad_mode == NGT_GRAD_EXACT && a->fwd.blending_mode == NGT_BEER_LAMBERT && cb > 1;
+}
+
 extern "C" size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* a) {
-  if (!a || a->grad_mode != NGT_GRAD_REFERENCE) return 0;
+  if (!a) return 0;
+  if (a->grad_mode != NGT_GRAD_REFERENCE) return needs_sign_flag(a) ? 256 : 0;
   const int64_t vox = a->fwd.input_shape[1] * a->fwd.input_shape[2] * a->fwd.input_shape[3];
   const int64_t cin = a->fwd.input_shape[4];
   return size_t(vox * (cin + 1)) * compute_size(a->fwd.dtype);
@@ -552,9 +648,23 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
   const int slots = num_slots(p);
   if (a->grad_mode == NGT_GRAD_EXACT) {
+    const bool bl = needs_sign_flag(a);
+    if (bl) {
+      if (!a->workspace || a->workspace_bytes < 256)
+        return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: exact Beer-Lambert mode needs 256 workspace bytes");
+      if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: exact Beer-Lambert mode needs the forward output");
+      p.flag = static_cast<const int*>(a->workspace);
+      if (cudaMemsetAsync(a->workspace, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_bwd memset");
+      rc = launch_dtype(a->fwd.dtype, SIGN, cin, cb, dim3(1), st, p);
+      if (rc) return rc;
+    }
     for (int s0 = 0; s0 < slots; s0 += 65535) {
       p.slot0 = s0;
       const dim3 grid(tiles, min(65535, slots - s0));
+      if (bl) {
+        rc = launch_dtype(a->fwd.dtype, BWD_BL, cin, cb, grid, st, p);
+        if (rc) return rc;
+      }
       rc = launch_dtype(a->fwd.dtype, BWD_EXACT, cin, cb, grid, st, p);
       if (rc) return rc;
     }

@@ -293,10 +293,11 @@ __device__ __forceinline__ void xf_slot(const XfParams<T>& p, int slot, int& b, 
 template <int C, class T>
 __global__ void __launch_bounds__(kBlock) k_xf_fwd(XfParams<T> p) {
   __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
   const int slot = p.slot0 + blockIdx.y;
   int b, c;
   xf_slot(p, slot, b, c);
-  if (threadIdx.x == 0) build_cam(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam);
+  if (threadIdx.x < 32) build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, cam_sh);
   __syncthreads();
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t osz = p.dout.count();
@@ -316,10 +317,11 @@ __global__ void __launch_bounds__(kBlock) k_xf_fwd(XfParams<T> p) {
 template <int C, class T>
 __global__ void __launch_bounds__(kBlock) k_xf_bwd(XfParams<T> p, int reference) {
   __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
   const int slot = p.slot0 + blockIdx.y;
   int b, c;
   xf_slot(p, slot, b, c);
-  if (threadIdx.x == 0) build_cam(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam);
+  if (threadIdx.x < 32) build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, cam_sh);
   __syncthreads();
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t osz = p.dout.count();
@@ -377,8 +379,9 @@ __global__ void k_mip_down(const T* __restrict__ in, T* __restrict__ out, Dims d
 __global__ void k_lod(const float* MV, const float* P, const float* F, Dims din, Dims dout, int cm, int relative,
                       float* out) {
   __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
   const int v = blockIdx.y;
-  if (threadIdx.x == 0) build_cam(nullptr, MV + 16 * v, P + 16 * v, F + 6 * v, cam);
+  if (threadIdx.x < 32) build_cam_warp(nullptr, MV + 16 * v, P + 16 * v, F + 6 * v, cam, cam_sh);
   __syncthreads();
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t osz = dout.count();
