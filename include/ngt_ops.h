@@ -195,6 +195,11 @@ typedef struct {
    * formed on the fly instead of materialised. 0 = off (Cb = C). */
   int32_t emission_channels;
   float emission_scale[4];
+  /* Forward scratch for the quad gather layout of a one-channel LINEAR input
+   * (size from ngt_raymarch_fwd_workspace_bytes; null: direct gathers, same
+   * results).  Unused by the backward, which takes its own workspace. */
+  void* workspace;
+  size_t workspace_bytes;
 } ngt_raymarch_args;
 
 typedef struct {
@@ -204,11 +209,15 @@ typedef struct {
   void* input_grad;           /* shape of fwd.input (float32/64) */
   int32_t grad_mode;
   void* workspace;            /* reference mode: gradient buffer + sample-weight sums;
-                                 exact Beer-Lambert: an extinction-sign flag
-                                 (size from ngt_raymarch_bwd_workspace_bytes) */
+                                 exact mode: an extinction-sign flag (Beer-Lambert)
+                                 and, for a one-channel float / 16-bit input, the
+                                 quad layout and its gradient accumulator (size
+                                 from ngt_raymarch_bwd_workspace_bytes; 256 bytes
+                                 select direct gathers and scatters) */
   size_t workspace_bytes;
 } ngt_raymarch_grad_args;
 
+size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* args);
 int ngt_raymarch_fwd(const ngt_raymarch_args* args, void* stream);
 int ngt_raymarch_bwd(const ngt_raymarch_grad_args* args, void* stream);
 size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* args);

@@ -492,9 +492,7 @@ __device__ __forceinline__ void scatter_quadratic_counted(S* __restrict__ grad, 
 
 // -------------------------------------------------------------- camera math
 // Matrices enter as 16 floats read column-major (transformations.hpp:42-47).
-// Per (batch, camera) the kernels need MV = V*M, its inverse and P, P^-1; they
-// are formed in double and rounded to float (the reference inverts in float on
-// the host, transformations.hpp:48-68).
+// Per (batch, camera) the kernels need MV = V*M, its inverse and P, P^-1.
 struct Cam {
   float mv[16], mvi[16], p[16], pi[16];  // row-major: m[r*4+c]
   float near_, far_;
@@ -507,22 +505,17 @@ __device__ __forceinline__ double det3(double a, double b, double c, double d, d
 }
 
 __device__ __forceinline__ double cofactor4(const double* m, int i, int j) {
-  double s[9];
-  int k = 0;
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-      if (r != i && c != j) s[k++] = m[r * 4 + c];
-  const double d = det3(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8]);
+  const int r0 = i == 0 ? 1 : 0, r1 = i <= 1 ? 2 : 1, r2 = i <= 2 ? 3 : 2;
+  const int c0 = j == 0 ? 1 : 0, c1 = j <= 1 ? 2 : 1, c2 = j <= 2 ? 3 : 2;
+  const double d = det3(m[r0 * 4 + c0], m[r0 * 4 + c1], m[r0 * 4 + c2], m[r1 * 4 + c0], m[r1 * 4 + c1],
+                        m[r1 * 4 + c2], m[r2 * 4 + c0], m[r2 * 4 + c1], m[r2 * 4 + c2]);
   return ((i + j) & 1) ? -d : d;
 }
 
 // Element (r, c) of the inverse by the adjugate: C_cr / det, det expanded along row 0.
 __device__ __forceinline__ double inverse_element(const double* m, int r, int c) {
-  double det = 0.0;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) det += m[j] * cofactor4(m, 0, j);
+  const double det = m[0] * cofactor4(m, 0, 0) + m[1] * cofactor4(m, 0, 1) + m[2] * cofactor4(m, 0, 2) +
+                     m[3] * cofactor4(m, 0, 3);
   return cofactor4(m, c, r) / det;
 }
 
@@ -533,9 +526,10 @@ struct CamScratch {
 
 // Forms ``cam`` cooperatively with the 32 lanes of the calling warp (every lane
 // must call it): lanes 0-15 one element each of MV = V*M and of MV^-1, lanes
-// 16-31 one element each of P^-1, all in double and rounded to float.  M16 may
-// be null (identity model matrix).  Inputs are column-major (as the reference's
-// setTransformations reads them); Cam holds row-major matrices.
+// 16-31 one element each of P^-1, in double and rounded to float.  M16 may be
+// null (identity model matrix).  Inputs are column-major (the reference's
+// setTransformations, transformations.hpp:48-68, reads them so); Cam holds
+// row-major matrices.
 __device__ inline void build_cam_warp(const float* M16, const float* V16, const float* P16, const float* F6,
                                       Cam& cam, CamScratch& sh) {
   const int lane = threadIdx.x & 31;
@@ -548,9 +542,8 @@ __device__ inline void build_cam_warp(const float* M16, const float* V16, const 
   }
   __syncwarp();
   if (lane < 16) {
-    double s = 0.0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) s += sh.V[r * 4 + k] * sh.M[k * 4 + c];
+    const double s = sh.V[r * 4 + 0] * sh.M[0 * 4 + c] + sh.V[r * 4 + 1] * sh.M[1 * 4 + c] +
+                     sh.V[r * 4 + 2] * sh.M[2 * 4 + c] + sh.V[r * 4 + 3] * sh.M[3 * 4 + c];
     sh.MV[e] = s;
     cam.mv[e] = (float)s;
   } else {

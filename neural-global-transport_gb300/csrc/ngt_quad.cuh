@@ -1,0 +1,232 @@
+// Padded (x, y)-quad layout of a one-channel grid for trilinear gathers and
+// scatters: two 16-byte (float) or 8-byte (16-bit) accesses per sample instead
+// of eight scattered 4-byte ones.
+//
+// Entry (xq, yq, zq) of a W x H x D grid, xq in [0, W], yq in [0, H], zq in
+// [0, D + 1], holds the four cells (x0, y0), (x0 + 1, y0), (x0, y0 + 1),
+// (x0 + 1, y0 + 1) of plane z with x0 = xq - 1, y0 = yq - 1, z = zq - 1, in the
+// reference's corner order (x fastest, then y).  The boundary rule is applied
+// to every corner when the quads are built: BORDER reads 0 outside the grid,
+// CLAMP the clamped cell, WRAP the wrapped cell.  A trilinear sample with lower
+// corner (x0, y0, z0) reads entry (x0 + 1, y0 + 1) of planes z0 + 1 and z0 + 2,
+// after the lower corner is normalised per axis (BORDER: already in [-1, n-1]
+// for a sample inside the grid; CLAMP: clamped to [-1, n-1]; WRAP: wrapped to
+// [0, n-1]).  The interpolation weights and the lerp order are those of
+// read_linear, and the upper corner there is ceil(p) where this layout uses
+// floor(p) + 1; the two differ only when the weight of that corner is 0, so for
+// finite data the samples are identical.
+//
+// The adjoint accumulates into a float4 quad grid of the same shape (one
+// vector atomic per plane); k_quad_fold then sums, for every cell, the four
+// quad components that hold it (plus, for CLAMP and WRAP, the padded entries
+// whose corner maps onto it).
+#pragma once
+
+#include "ngt_common.cuh"
+
+namespace ngt {
+
+template <class T> struct QuadOf;
+template <> struct QuadOf<float> { typedef float4 type; };
+template <> struct QuadOf<__nv_bfloat16> { typedef uint2 type; };
+template <> struct QuadOf<__half> { typedef uint2 type; };
+
+struct QuadDims {
+  int x, y, z;          // W + 1, H + 1, D + 2
+  int64_t plane, count;  // entries per plane, per grid
+  __device__ __host__ static QuadDims of(const Dims& d) {
+    QuadDims q;
+    q.x = d.x + 1;
+    q.y = d.y + 1;
+    q.z = d.z + 2;
+    q.plane = int64_t(q.x) * q.y;
+    q.count = q.plane * q.z;
+    return q;
+  }
+};
+
+__device__ __forceinline__ int quad_cell(int i, int n, int bm, bool& valid) {
+  valid = true;
+  if (bm == BORDER) {
+    valid = i >= 0 && i < n;
+    return valid ? i : 0;
+  }
+  if (bm == CLAMP) return min(max(i, 0), n - 1);
+  return wrap_index(i, n);
+}
+
+template <class T>
+__device__ __forceinline__ uint32_t raw16(T v) {
+  return uint32_t(*reinterpret_cast<const uint16_t*>(&v));
+}
+
+// One thread per entry; batch b of N grids at blockIdx.y.
+template <class T>
+__global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename QuadOf<T>::type* __restrict__ q) {
+  const QuadDims qd = QuadDims::of(d);
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= qd.count) return;
+  const int b = blockIdx.y;
+  const int xq = int(e % qd.x), yq = int((e / qd.x) % qd.y), zq = int(e / qd.plane);
+  bool vz;
+  const int z = quad_cell(zq - 1, d.z, bm, vz);
+  T v[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    bool vx, vy;
+    const int x = quad_cell(xq - 1 + (k & 1), d.x, bm, vx);
+    const int y = quad_cell(yq - 1 + (k >> 1), d.y, bm, vy);
+    const T* src = g + int64_t(b) * d.count() + flat(x, y, z, d);
+    v[k] = (vx && vy && vz) ? *src : T(0.0f);
+  }
+  typename QuadOf<T>::type o;
+  if constexpr (sizeof(T) == 4) {
+    o = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    o.x = raw16(v[0]) | (raw16(v[1]) << 16);
+    o.y = raw16(v[2]) | (raw16(v[3]) << 16);
+  }
+  q[int64_t(b) * qd.count + e] = o;
+}
+
+template <class T>
+__device__ __forceinline__ T from_raw16(uint32_t r) {
+  const uint16_t h = uint16_t(r);
+  return *reinterpret_cast<const T*>(&h);
+}
+
+__device__ __forceinline__ void quad_load(const float4* q, int64_t i, float v[4]) {
+  const float4 a = __ldg(q + i);
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+}
+
+template <class T>
+__device__ __forceinline__ void quad_load16(const uint2* q, int64_t i, float v[4]) {
+  const uint2 a = __ldg(q + i);
+  v[0] = float(from_raw16<T>(a.x & 0xffffu));
+  v[1] = float(from_raw16<T>(a.x >> 16));
+  v[2] = float(from_raw16<T>(a.y & 0xffffu));
+  v[3] = float(from_raw16<T>(a.y >> 16));
+}
+
+template <class T>
+__device__ __forceinline__ void quad_fetch(const typename QuadOf<T>::type* q, int64_t i, float v[4]) {
+  if constexpr (sizeof(T) == 4)
+    quad_load(q, i, v);
+  else
+    quad_load16<T>(q, i, v);
+}
+
+// Lower corner and weights of a trilinear sample (tri_setup's arithmetic);
+// returns false when BORDER puts the sample outside the grid (it reads 0).
+struct QuadPos {
+  int64_t idx;  // entry of plane z0 + 1
+  float w[3];
+};
+
+__device__ __forceinline__ bool quad_setup(float px, float py, float pz, const Dims& d, const QuadDims& qd, int bm,
+                                           QuadPos& s) {
+  const float p[3] = {px, py, pz};
+  const int n[3] = {d.x, d.y, d.z};
+  int i0[3];
+  bool inside = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float f = floorf(p[a]);
+    s.w[a] = sub_rn(p[a], f);
+    int i = to_int_rz(f);
+    if (bm == BORDER) {
+      const float q = add_rn(p[a], 0.5f);
+      inside = inside && (q >= 0.0f) && (q < float(n[a]));
+    } else if (bm == CLAMP) {
+      i = min(max(i, -1), n[a] - 1);
+    } else {
+      i = wrap_index(i, n[a]);
+    }
+    i0[a] = i;
+  }
+  if (!inside) return false;
+  s.idx = (int64_t(i0[2] + 1) * qd.y + (i0[1] + 1)) * qd.x + (i0[0] + 1);
+  return true;
+}
+
+template <class T>
+__device__ __forceinline__ float read_linear_quad(const typename QuadOf<T>::type* __restrict__ q, float px, float py,
+                                                  float pz, const Dims& d, const QuadDims& qd, int bm) {
+  QuadPos s;
+  if (!quad_setup(px, py, pz, d, qd, bm, s)) return 0.0f;
+  float a[4], b[4];
+  quad_fetch<T>(q, s.idx, a);
+  quad_fetch<T>(q, s.idx + qd.plane, b);
+  const float v0 = lerp_rn(lerp_rn(a[0], a[1], s.w[0]), lerp_rn(a[2], a[3], s.w[0]), s.w[1]);
+  const float v1 = lerp_rn(lerp_rn(b[0], b[1], s.w[0]), lerp_rn(b[2], b[3], s.w[0]), s.w[1]);
+  return lerp_rn(v0, v1, s.w[2]);
+}
+
+// Adjoint of read_linear_quad: g times the eight corner weights (tri_weight's
+// products) added to the quad gradient grid with two vector atomics.
+__device__ __forceinline__ void scatter_linear_quad(float4* __restrict__ gq, float px, float py, float pz,
+                                                    const Dims& d, const QuadDims& qd, int bm, float g) {
+  QuadPos s;
+  if (!quad_setup(px, py, pz, d, qd, bm, s)) return;
+  const float wx1 = s.w[0], wx0 = sub_rn(1.0f, s.w[0]);
+  const float wy1 = s.w[1], wy0 = sub_rn(1.0f, s.w[1]);
+  const float wz1 = s.w[2], wz0 = sub_rn(1.0f, s.w[2]);
+  const float a00 = mul_rn(wx0, wy0), a10 = mul_rn(wx1, wy0), a01 = mul_rn(wx0, wy1), a11 = mul_rn(wx1, wy1);
+  atomicAdd(gq + s.idx, make_float4(mul_rn(g, mul_rn(a00, wz0)), mul_rn(g, mul_rn(a10, wz0)),
+                                    mul_rn(g, mul_rn(a01, wz0)), mul_rn(g, mul_rn(a11, wz0))));
+  atomicAdd(gq + s.idx + qd.plane, make_float4(mul_rn(g, mul_rn(a00, wz1)), mul_rn(g, mul_rn(a10, wz1)),
+                                               mul_rn(g, mul_rn(a01, wz1)), mul_rn(g, mul_rn(a11, wz1))));
+}
+
+// Coordinates of an axis of n cells whose boundary rule maps onto cell i: i
+// itself, plus the padding coordinates -1 / n that CLAMP or WRAP send to i.
+// Returns the count (at most 3, for n == 1).
+__device__ __forceinline__ int quad_sources(int i, int n, int bm, int src[3]) {
+  int k = 0;
+  src[k++] = i;
+  if (bm == CLAMP) {
+    if (i == 0) src[k++] = -1;
+    if (i == n - 1) src[k++] = n;
+  } else if (bm == WRAP) {
+    if (i == 0) src[k++] = n;
+    if (i == n - 1) src[k++] = -1;
+  }
+  return k;
+}
+
+// Cell gradients from the quad gradient grid, written (not added) to grad; one
+// thread per cell, batch at blockIdx.y.  Component (kx, ky) of entry (xq, yq) is coordinate
+// (xq - 1 + kx, yq - 1 + ky) of plane zq - 1.
+__global__ void k_quad_fold(const float4* __restrict__ gq, Dims d, int bm, float* __restrict__ grad) {
+  const QuadDims qd = QuadDims::of(d);
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= d.count()) return;
+  const int b = blockIdx.y;
+  const float4* q = gq + int64_t(b) * qd.count;
+  const int x = int(i % d.x), y = int((i / d.x) % d.y), z = int(i / (int64_t(d.x) * d.y));
+  int sx[3], sy[3], sz[3];
+  const int nx = quad_sources(x, d.x, bm, sx), ny = quad_sources(y, d.y, bm, sy), nz = quad_sources(z, d.z, bm, sz);
+  float acc = 0.0f;
+  for (int kz = 0; kz < nz; ++kz) {
+    const int64_t pz = int64_t(sz[kz] + 1) * qd.plane;
+    for (int ky = 0; ky < ny; ++ky) {
+      const int cy = sy[ky];
+      for (int kx = 0; kx < nx; ++kx) {
+        const int cx = sx[kx];
+        // (cx, cy) is component (0,0) of entry (cx+1, cy+1), (1,0) of (cx, cy+1),
+        // (0,1) of (cx+1, cy), (1,1) of (cx, cy); entries outside [0,W]x[0,H] do not exist
+        if (cx + 1 <= d.x && cy + 1 <= d.y) acc += q[pz + int64_t(cy + 1) * qd.x + (cx + 1)].x;
+        if (cx >= 0 && cy + 1 <= d.y) acc += q[pz + int64_t(cy + 1) * qd.x + cx].y;
+        if (cx + 1 <= d.x && cy >= 0) acc += q[pz + int64_t(cy) * qd.x + (cx + 1)].z;
+        if (cx >= 0 && cy >= 0) acc += q[pz + int64_t(cy) * qd.x + cx].w;
+      }
+    }
+  }
+  grad[int64_t(b) * d.count() + i] = acc;
+}
+
+}  // namespace ngt

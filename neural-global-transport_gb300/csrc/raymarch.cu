@@ -15,6 +15,7 @@
 #include "ngt_common.cuh"
 #include "ngt_host.cuh"
 #include "ngt_blend.cuh"
+#include "ngt_quad.cuh"
 
 namespace ngt {
 namespace {
@@ -40,7 +41,29 @@ struct RayParams {
   float scale[4];
   int slot0;             // first (batch, camera) slot of this launch
   const int* flag;       // exact Beer-Lambert backward: nonzero if an extinction sample can be negative
+  const Cam* cams;       // per-slot cameras formed by k_build_cams, or null (each block forms its own)
+  const void* quad;      // quad layout of the input (one channel, LINEAR) or null
+  float4* gquad;         // quad gradient accumulator (exact backward) or null
+  QuadDims qd;
 };
+
+// One-channel float / 16-bit grids sampled LINEAR go through the quad layout.
+template <int CIN, class T>
+constexpr bool quad_able() {
+  return CIN == 1 && !std::is_same<T, double>::value;
+}
+
+template <int CIN, class T>
+__device__ __forceinline__ const void* quad_of(const RayParams& p, int b) {
+  if constexpr (quad_able<CIN, T>())
+    return p.quad ? static_cast<const void*>(static_cast<const typename QuadOf<T>::type*>(p.quad) + int64_t(b) * p.qd.count)
+                  : nullptr;
+  return nullptr;
+}
+
+__device__ __forceinline__ float4* gquad_of(const RayParams& p, int b) {
+  return p.gquad ? p.gquad + int64_t(b) * p.qd.count : nullptr;
+}
 
 __device__ __forceinline__ void slot_to_bc(const RayParams& p, int slot, int& b, int& c, int& oslot) {
   if (p.sep) {
@@ -126,10 +149,18 @@ __device__ inline Ray ray_setup(const Cam& cam, int px, int py, const RayParams&
 
 // Sample CIN channels at object-space position pos and expand to CB blend channels.
 template <int CIN, int CB, class T, class S>
-__device__ __forceinline__ void sample_cell(const T* __restrict__ g, const float pos[3], const RayParams& p,
-                                            S cell[CB]) {
+__device__ __forceinline__ void sample_cell(const T* __restrict__ g, const void* qg, const float pos[3],
+                                            const RayParams& p, S cell[CB]) {
   const S px = S(pos[0] - 0.5f), py = S(pos[1] - 0.5f), pz = S(pos[2] - 0.5f);
   S v[CIN];
+  if constexpr (quad_able<CIN, T>()) {
+    if (qg) {
+      v[0] = read_linear_quad<T>(static_cast<const typename QuadOf<T>::type*>(qg), px, py, pz, p.din, p.qd, p.bm);
+#pragma unroll
+      for (int c = 0; c < CB; ++c) cell[c] = (CIN == CB) ? v[0] : S(p.scale[c]) * v[0];
+      return;
+    }
+  }
   if (p.fm == LINEAR) {
     read_linear<CIN>(g, px, py, pz, p.din, p.bm, v);
   } else if (p.fm == NEAREST) {
@@ -149,9 +180,18 @@ __device__ __forceinline__ void sample_cell(const T* __restrict__ g, const float
 }
 
 template <int CIN, int CB, class S>
-__device__ __forceinline__ void scatter_cell(const RayParams& p, S* __restrict__ grad, const float pos[3],
+__device__ __forceinline__ void scatter_cell(const RayParams& p, S* __restrict__ grad, float4* gq, const float pos[3],
                                              const S dcell[CB]) {
   const S px = S(pos[0] - 0.5f), py = S(pos[1] - 0.5f), pz = S(pos[2] - 0.5f);
+  if constexpr (CIN == 1 && std::is_same<S, float>::value) {
+    if (gq) {
+      S g = S(0);
+#pragma unroll
+      for (int c = 0; c < CB; ++c) g += (CIN == CB) ? dcell[c] : S(p.scale[c]) * dcell[c];
+      scatter_linear_quad(gq, px, py, pz, p.din, p.qd, p.bm, g);
+      return;
+    }
+  }
   if (CIN == CB) {
     S g[CIN];
 #pragma unroll
@@ -166,8 +206,28 @@ __device__ __forceinline__ void scatter_cell(const RayParams& p, S* __restrict__
 }
 
 // The block's camera, formed by warp 0; the caller synchronises the block.
-__device__ __forceinline__ void load_cam(const RayParams& p, int b, int c, Cam& cam, CamScratch& sh) {
-  if (threadIdx.x < 32) build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, sh);
+__device__ __forceinline__ void load_cam(const RayParams& p, int slot, int b, int c, Cam& cam, CamScratch& sh) {
+  if (p.cams) {
+    const float* src = reinterpret_cast<const float*>(p.cams + slot);
+    float* dst = reinterpret_cast<float*>(&cam);
+    for (int i = threadIdx.x; i < int(sizeof(Cam) / sizeof(float)); i += blockDim.x) dst[i] = __ldg(src + i);
+  } else if (threadIdx.x < 32) {
+    build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, sh);
+  }
+}
+
+// Every (batch, camera) slot's camera, one warp per slot, formed once per call
+// into ``cams`` for the raymarch blocks to copy.
+__global__ void k_build_cams(RayParams p, Cam* __restrict__ cams) {
+  __shared__ Cam cam;
+  __shared__ CamScratch sh;
+  int b, c, oslot;
+  slot_to_bc(p, blockIdx.x, b, c, oslot);
+  build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, sh);
+  __syncwarp();
+  const float* src = reinterpret_cast<const float*>(&cam);
+  float* dst = reinterpret_cast<float*>(cams + blockIdx.x);
+  for (int i = threadIdx.x; i < int(sizeof(Cam) / sizeof(float)); i += 32) dst[i] = src[i];
 }
 
 // ----------------------------------------------------------------- forward
@@ -177,7 +237,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
   __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, b, c, cam, cam_sh);
+  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
   __syncthreads();
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
   int px, py;
@@ -186,6 +246,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
   py += (blockIdx.x / tiles_x) * kTileY;
   if (px >= p.W || py >= p.H) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  const void* qg = quad_of<CIN, T>(p, b);
   const Ray r = ray_setup(cam, px, py, p);
   S acc[CB];
 #pragma unroll
@@ -194,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
     float pos[3] = {r.s[0], r.s[1], r.s[2]};
     for (int i = 0; i < r.steps; ++i) {
       S cell[CB];
-      sample_cell<CIN, CB>(g, pos, p, cell);
+      sample_cell<CIN, CB>(g, qg, pos, p, cell);
       blend_step<CB>(acc, cell, p.blend);
 #pragma unroll
       for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
@@ -211,11 +272,12 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
 // uses the forward's own positions and densities, not a subtraction.
 template <int CIN, int CB, class T, class S>
 __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
+  if (p.flag && *p.flag == 0) return;  // Beer-Lambert with non-negative extinction: k_raymarch_bwd_bl
   __shared__ Cam cam;
   __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, b, c, cam, cam_sh);
+  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
   __syncthreads();
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
   int px, py;
@@ -224,10 +286,11 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
   py += (blockIdx.x / tiles_x) * kTileY;
   if (px >= p.W || py >= p.H) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  const void* qg = quad_of<CIN, T>(p, b);
   S* grad = reinterpret_cast<S*>(p.in_grad) + int64_t(b) * p.din.count() * CIN;
+  float4* gq = gquad_of(p, b);
   const Ray r = ray_setup(cam, px, py, p);
   if (!r.hit || r.steps <= 0) return;
-  if (p.flag && *p.flag == 0) return;  // Beer-Lambert with non-negative extinction: k_raymarch_bwd_bl
   S G[CB];
   const S* og = reinterpret_cast<const S*>(p.out_grad) + ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
 #pragma unroll
@@ -238,9 +301,9 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
     float pos[3] = {r.s[0], r.s[1], r.s[2]};
     for (int i = 0; i < r.steps; ++i) {
       S cell[CB], dcell[CB];
-      sample_cell<CIN, CB>(g, pos, p, cell);
+      sample_cell<CIN, CB>(g, qg, pos, p, cell);
       blend_adjoint<CB>(G, cell, S(0), p.blend, dcell);
-      scatter_cell<CIN, CB>(p, grad, pos, dcell);
+      scatter_cell<CIN, CB>(p, grad, gq, pos, dcell);
 #pragma unroll
       for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
     }
@@ -265,7 +328,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
         ck_a[k] = a;
       }
       S cell[CB];
-      sample_cell<CIN, CB>(g, pos, p, cell);
+      sample_cell<CIN, CB>(g, qg, pos, p, cell);
       a = state_update(a, cell[CB - 1], p.blend);
 #pragma unroll
       for (int q = 0; q < 3; ++q) pos[q] += r.st[q];
@@ -283,7 +346,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
       S a = ck_a[seg];
       for (int i = i0; i < j0; ++i) {  // re-march to the sub-segment start (only when K > kSeg)
         S cell[CB];
-        sample_cell<CIN, CB>(g, pos, p, cell);
+        sample_cell<CIN, CB>(g, qg, pos, p, cell);
         a = state_update(a, cell[CB - 1], p.blend);
 #pragma unroll
         for (int q = 0; q < 3; ++q) pos[q] += r.st[q];
@@ -294,7 +357,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
         buf_pos[j][1] = pos[1];
         buf_pos[j][2] = pos[2];
         buf_a[j] = a;
-        sample_cell<CIN, CB>(g, pos, p, buf_cell[j]);
+        sample_cell<CIN, CB>(g, qg, pos, p, buf_cell[j]);
         a = state_update(a, buf_cell[j][CB - 1], p.blend);
 #pragma unroll
         for (int q = 0; q < 3; ++q) pos[q] += r.st[q];
@@ -302,7 +365,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
       for (int j = j1 - j0 - 1; j >= 0; --j) {
         S dcell[CB];
         blend_adjoint<CB>(G, buf_cell[j], buf_a[j], p.blend, dcell);
-        scatter_cell<CIN, CB>(p, grad, buf_pos[j], dcell);
+        scatter_cell<CIN, CB>(p, grad, gq, buf_pos[j], dcell);
       }
     }
   }
@@ -326,7 +389,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_bl(RayParams p) {
   __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, b, c, cam, cam_sh);
+  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
   __syncthreads();
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
   int px, py;
@@ -335,7 +398,9 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_bl(RayParams p) {
   py += (blockIdx.x / tiles_x) * kTileY;
   if (px >= p.W || py >= p.H) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  const void* qg = quad_of<CIN, T>(p, b);
   S* grad = reinterpret_cast<S*>(p.in_grad) + int64_t(b) * p.din.count() * CIN;
+  float4* gq = gquad_of(p, b);
   const Ray r = ray_setup(cam, px, py, p);
   if (!r.hit || r.steps <= 0) return;
   const int64_t o = ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
@@ -350,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_bl(RayParams p) {
   float pos[3] = {r.s[0], r.s[1], r.s[2]};
   for (int i = 0; i < r.steps; ++i) {
     S cell[CB], dcell[CB];
-    sample_cell<CIN, CB>(g, pos, p, cell);
+    sample_cell<CIN, CB>(g, qg, pos, p, cell);
     d = d + cell[CB - 1];
     const S t = ex(-d);
     S lg = S(0);
@@ -361,7 +426,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_bl(RayParams p) {
     }
     dcell[CB - 1] = gD - (lgf - w);
     w += t * lg;
-    scatter_cell<CIN, CB>(p, grad, pos, dcell);
+    scatter_cell<CIN, CB>(p, grad, gq, pos, dcell);
 #pragma unroll
     for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
   }
@@ -429,7 +494,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_reference(RayParams p
   __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, b, c, cam, cam_sh);
+  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
   __syncthreads();
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
   int px, py;
@@ -438,6 +503,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_reference(RayParams p
   py += (blockIdx.x / tiles_x) * kTileY;
   if (px >= p.W || py >= p.H) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
+  const void* qg = quad_of<CIN, T>(p, b);
   S* buf = reinterpret_cast<S*>(p.wbuf);
   S* wsum = reinterpret_cast<S*>(p.wsum);
   const Ray r = ray_setup(cam, px, py, p);
@@ -452,7 +518,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_reference(RayParams p
   float pos[3] = {r.e[0], r.e[1], r.e[2]};
   for (int i = r.steps - 1; i >= 0; --i) {
     S cell[CB], dcell[CB];
-    sample_cell<CIN, CB>(g, pos, p, cell);
+    sample_cell<CIN, CB>(g, qg, pos, p, cell);
     blend_grad_reference<CB>(G, cell, acc, p.blend, dcell);
     const S qx = S(pos[0] - 0.5f), qy = S(pos[1] - 0.5f), qz = S(pos[2] - 0.5f);
     if (CIN == CB) {
@@ -589,41 +655,154 @@ int launch_dtype(int dtype, int which, int cin, int cb, dim3 grid, cudaStream_t 
 
 size_t compute_size(int dtype) { return dtype == NGT_F64 ? 8 : 4; }
 
-}  // namespace
-}  // namespace ngt
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
-using namespace ngt;
-
-extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
-  int cin, cb;
-  int rc = validate(a, cin, cb);
-  if (rc) return rc;
-  if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null output");
-  RayParams p = make_params(a);
-  const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
-  const int slots = num_slots(p);
-  for (int s0 = 0; s0 < slots; s0 += 65535) {
-    p.slot0 = s0;
-    const dim3 grid(tiles, min(65535, slots - s0));
-    rc = launch_dtype(a->dtype, FWD, cin, cb, grid, as_stream(stream), p);
-    if (rc) return rc;
-  }
-  return check_launch("ngt_raymarch_fwd");
+Dims in_dims(const ngt_raymarch_args* a) {
+  return Dims{int(a->input_shape[3]), int(a->input_shape[2]), int(a->input_shape[1])};
 }
 
-// Exact Beer-Lambert backward: one int flag; reference: gradient buffer + weight sums.
+int64_t slots_of(const ngt_raymarch_args* a) {
+  return a->separate_camera_batch ? a->input_shape[0] * a->num_cameras : a->input_shape[0];
+}
+
+// One-channel LINEAR float / 16-bit inputs are gathered through the quad layout.
+bool quad_case(const ngt_raymarch_args* a) {
+  return a->input_shape[4] == 1 && a->interpolation == NGT_LINEAR && a->dtype != NGT_F64 &&
+         a->input_shape[0] <= 65535;
+}
+
+size_t quad_bytes(const ngt_raymarch_args* a) {
+  const QuadDims q = QuadDims::of(in_dims(a));
+  return align256(size_t(a->input_shape[0] * q.count) * (a->dtype == NGT_F32 ? 16 : 8));
+}
+
+size_t gquad_bytes(const ngt_raymarch_args* a) {
+  return align256(size_t(a->input_shape[0] * QuadDims::of(in_dims(a)).count) * 16);
+}
+
+size_t cams_bytes(const ngt_raymarch_args* a) { return align256(size_t(slots_of(a)) * sizeof(Cam)); }
+
+// Exact Beer-Lambert backward needs the extinction-sign flag.
 bool needs_sign_flag(const ngt_raymarch_grad_args* a) {
   const int cin = int(a->fwd.input_shape[4]);
   const int cb = a->fwd.emission_channels ? a->fwd.emission_channels : cin;
   return a->grad_mode == NGT_GRAD_EXACT && a->fwd.blending_mode == NGT_BEER_LAMBERT && cb > 1;
 }
 
+// Workspace layouts (offsets in bytes, 256-aligned).
+//   forward:            [cameras][quad input]
+//   backward, exact:    [sign flag 256][cameras][quad input][quad gradient]
+//   backward, reference:[cameras][gradient buffer][weight sums]
+struct Layout {
+  size_t flag, cams, quad, gquad, buf, wsum, total;
+};
+
+Layout fwd_layout(const ngt_raymarch_args* a) {
+  Layout l = {};
+  l.cams = 0;
+  l.quad = cams_bytes(a);
+  l.total = l.quad + (quad_case(a) ? quad_bytes(a) : 0);
+  return l;
+}
+
+Layout bwd_layout(const ngt_raymarch_grad_args* g) {
+  const ngt_raymarch_args* a = &g->fwd;
+  Layout l = {};
+  if (g->grad_mode == NGT_GRAD_REFERENCE) {
+    const int64_t vox = a->input_shape[1] * a->input_shape[2] * a->input_shape[3];
+    l.cams = 0;
+    l.buf = cams_bytes(a);
+    l.wsum = l.buf + align256(size_t(vox * a->input_shape[4]) * compute_size(a->dtype));
+    l.total = l.wsum + align256(size_t(vox) * compute_size(a->dtype));
+    return l;
+  }
+  l.flag = 0;
+  l.cams = 256;
+  l.quad = l.cams + cams_bytes(a);
+  l.gquad = l.quad + (quad_case(a) ? quad_bytes(a) : 0);
+  l.total = l.gquad + (quad_case(a) ? gquad_bytes(a) : 0);
+  return l;
+}
+
+int build_quad(const ngt_raymarch_args* a, void* q, cudaStream_t st) {
+  const Dims d = in_dims(a);
+  const QuadDims qd = QuadDims::of(d);
+  const dim3 grid(ceil_div_u(qd.count, 256), unsigned(a->input_shape[0]));
+  switch (a->dtype) {
+    case NGT_F32:
+      k_quad_build<float><<<grid, 256, 0, st>>>(static_cast<const float*>(a->input), d, a->boundary,
+                                                 static_cast<float4*>(q));
+      break;
+    case NGT_BF16:
+      k_quad_build<__nv_bfloat16><<<grid, 256, 0, st>>>(static_cast<const __nv_bfloat16*>(a->input), d,
+                                                         a->boundary, static_cast<uint2*>(q));
+      break;
+    case NGT_F16:
+      k_quad_build<__half><<<grid, 256, 0, st>>>(static_cast<const __half*>(a->input), d, a->boundary,
+                                                  static_cast<uint2*>(q));
+      break;
+    default:
+      return fail(NGT_ERR_UNSUPPORTED, "raymarch: quad layout needs float or 16-bit storage");
+  }
+  return NGT_OK;
+}
+
+void build_cams(RayParams& p, void* at, cudaStream_t st) {
+  Cam* cams = static_cast<Cam*>(at);
+  k_build_cams<<<unsigned(num_slots(p)), 32, 0, st>>>(p, cams);
+  p.cams = cams;
+}
+
+int launch_slots(int dtype, int which, int cin, int cb, int tiles, cudaStream_t st, RayParams& p) {
+  const int slots = num_slots(p);
+  for (int s0 = 0; s0 < slots; s0 += 65535) {
+    p.slot0 = s0;
+    const int rc = launch_dtype(dtype, which, cin, cb, dim3(tiles, min(65535, slots - s0)), st, p);
+    if (rc) return rc;
+  }
+  return NGT_OK;
+}
+
+}  // namespace
+}  // namespace ngt
+
+using namespace ngt;
+
+extern "C" size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* a) {
+  return a ? fwd_layout(a).total : 0;
+}
+
+// With a workspace the cameras are formed once per call and a one-channel
+// LINEAR input is gathered through the quad layout; without one every block
+// forms its camera and gathers directly (same results).
+extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
+  int cin, cb;
+  int rc = validate(a, cin, cb);
+  if (rc) return rc;
+  if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null output");
+  RayParams p = make_params(a);
+  cudaStream_t st = as_stream(stream);
+  if (a->workspace) {
+    const Layout l = fwd_layout(a);
+    if (a->workspace_bytes < l.total)
+      return fail(NGT_ERR_WORKSPACE, "raymarch: the forward workspace needs %zu bytes", l.total);
+    char* w = static_cast<char*>(a->workspace);
+    build_cams(p, w + l.cams, st);
+    if (quad_case(a)) {
+      rc = build_quad(a, w + l.quad, st);
+      if (rc) return rc;
+      p.quad = w + l.quad;
+      p.qd = QuadDims::of(p.din);
+    }
+  }
+  const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
+  rc = launch_slots(a->dtype, FWD, cin, cb, tiles, st, p);
+  if (rc) return rc;
+  return check_launch("ngt_raymarch_fwd");
+}
+
 extern "C" size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* a) {
-  if (!a) return 0;
-  if (a->grad_mode != NGT_GRAD_REFERENCE) return needs_sign_flag(a) ? 256 : 0;
-  const int64_t vox = a->fwd.input_shape[1] * a->fwd.input_shape[2] * a->fwd.input_shape[3];
-  const int64_t cin = a->fwd.input_shape[4];
-  return size_t(vox * (cin + 1)) * compute_size(a->fwd.dtype);
+  return a ? bwd_layout(a).total : 0;
 }
 
 extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
@@ -636,48 +815,58 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   if (!a->output_grad || !a->input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: null pointer");
   if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: invalid grad_mode");
+  if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: the forward output is required");
+  const Layout l = bwd_layout(a);
+  if (!a->workspace || a->workspace_bytes < l.total)
+    return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: needs %zu workspace bytes", l.total);
   RayParams p = make_params(&a->fwd);
   p.out_fwd = a->output;
   p.out_grad = a->output_grad;
   p.in_grad = a->input_grad;
   cudaStream_t st = as_stream(stream);
+  char* w = static_cast<char*>(a->workspace);
   const int64_t vox = p.din.count();
   const size_t cs = compute_size(a->fwd.dtype);
-  if (cudaMemsetAsync(a->input_grad, 0, size_t(p.N) * vox * cin * cs, st) != cudaSuccess)
-    return check_launch("raymarch_bwd memset");
   const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
-  const int slots = num_slots(p);
+  build_cams(p, w + l.cams, st);
+
   if (a->grad_mode == NGT_GRAD_EXACT) {
+    const bool quad = quad_case(&a->fwd);
+    if (quad) {
+      rc = build_quad(&a->fwd, w + l.quad, st);
+      if (rc) return rc;
+      p.quad = w + l.quad;
+      p.gquad = reinterpret_cast<float4*>(w + l.gquad);
+      p.qd = QuadDims::of(p.din);
+      if (cudaMemsetAsync(p.gquad, 0, gquad_bytes(&a->fwd), st) != cudaSuccess)
+        return check_launch("raymarch_bwd memset");
+    } else if (cudaMemsetAsync(a->input_grad, 0, size_t(p.N) * vox * cin * cs, st) != cudaSuccess) {
+      return check_launch("raymarch_bwd memset");
+    }
     const bool bl = needs_sign_flag(a);
     if (bl) {
-      if (!a->workspace || a->workspace_bytes < 256)
-        return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: exact Beer-Lambert mode needs 256 workspace bytes");
-      if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: exact Beer-Lambert mode needs the forward output");
-      p.flag = static_cast<const int*>(a->workspace);
-      if (cudaMemsetAsync(a->workspace, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_bwd memset");
+      p.flag = reinterpret_cast<const int*>(w + l.flag);
+      if (cudaMemsetAsync(w + l.flag, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_bwd memset");
       rc = launch_dtype(a->fwd.dtype, SIGN, cin, cb, dim3(1), st, p);
       if (rc) return rc;
-    }
-    for (int s0 = 0; s0 < slots; s0 += 65535) {
-      p.slot0 = s0;
-      const dim3 grid(tiles, min(65535, slots - s0));
-      if (bl) {
-        rc = launch_dtype(a->fwd.dtype, BWD_BL, cin, cb, grid, st, p);
-        if (rc) return rc;
-      }
-      rc = launch_dtype(a->fwd.dtype, BWD_EXACT, cin, cb, grid, st, p);
+      rc = launch_slots(a->fwd.dtype, BWD_BL, cin, cb, tiles, st, p);
       if (rc) return rc;
     }
+    rc = launch_slots(a->fwd.dtype, BWD_EXACT, cin, cb, tiles, st, p);
+    if (rc) return rc;
+    if (quad)
+      k_quad_fold<<<dim3(ceil_div_u(vox, 256), unsigned(p.N)), 256, 0, st>>>(p.gquad, p.din, p.bm,
+                                                                            static_cast<float*>(a->input_grad));
     return check_launch("ngt_raymarch_bwd");
   }
+
   // reference: one (batch, camera) at a time, normalised by summed weights per camera
-  if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: reference mode needs the forward output");
-  const size_t need = ngt_raymarch_bwd_workspace_bytes(a);
-  if (!a->workspace || a->workspace_bytes < need)
-    return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: reference mode needs %zu workspace bytes", need);
-  p.wbuf = a->workspace;
-  p.wsum = static_cast<char*>(a->workspace) + size_t(vox * cin) * cs;
-  if (cudaMemsetAsync(a->workspace, 0, need, st) != cudaSuccess) return check_launch("raymarch_bwd memset");
+  if (cudaMemsetAsync(a->input_grad, 0, size_t(p.N) * vox * cin * cs, st) != cudaSuccess)
+    return check_launch("raymarch_bwd memset");
+  p.wbuf = w + l.buf;
+  p.wsum = w + l.wsum;
+  if (cudaMemsetAsync(w + l.buf, 0, l.total - l.buf, st) != cudaSuccess) return check_launch("raymarch_bwd memset");
+  const int slots = num_slots(p);
   for (int s = 0; s < slots; ++s) {
     p.slot0 = s;
     const int b = p.sep ? s / p.ncam : s;

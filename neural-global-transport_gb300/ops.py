@@ -358,6 +358,8 @@ def _ray_out_shape(input, V, out_dhw, a):
 def _ray_forward(input, M, V, P, F, out_dhw, a):
     out = torch.empty(_ray_out_shape(input, V, out_dhw, a), dtype=compute_dtype(input), device=input.device)
     r = _ray_args(input, M, V, P, F, out_dhw, out, a)
+    ws = _workspace(L.load().ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r)), input.device)
+    r.workspace, r.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
     L.call("ngt_raymarch_fwd", ctypes.byref(r), _stream())
     return out
 

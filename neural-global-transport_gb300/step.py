@@ -23,7 +23,10 @@ from .ops import _code, _ptr
 
 
 class RenderAdvectStep:
-    KERNELS_PER_STEP = 8  # advect 2, raymarch fwd, loss, raymarch bwd, advect bwd 3
+    # kernels of one f32 exact Beer-Lambert step: advect fwd 2, raymarch fwd 3 (cameras,
+    # quad layout, march), loss 1, raymarch bwd 6 (cameras, quad layout, sign check,
+    # one-pass and checkpointed marches, fold), advect bwd 3
+    KERNELS_PER_STEP = 15
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact"):
@@ -85,6 +88,9 @@ class RenderAdvectStep:
         r.blending_mode, r.keep_dims, r.separate_camera_batch = L.BLEND["BEER_LAMBERT"], 0, 1
         r.emission_channels = 2
         r.emission_scale[0], r.emission_scale[1] = self.emission
+        self.ray_fws = torch.empty(int(self.lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))),
+                                   dtype=torch.uint8, device=dev)
+        r.workspace, r.workspace_bytes = _ptr(self.ray_fws), self.ray_fws.numel()
         self.ray = r
         rg = L.RaymarchGradArgs()
         rg.fwd = r

@@ -472,6 +472,8 @@ def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v,
         if grad_mode == "exact":
             pos = _ray_positions(start, step, steps, dt)
             n = pos.shape[0]
+            if n == 0:  # every ray of this camera misses the clip box
+                continue
             cells = np.stack([_v2_sample(x[b], pos[i], interpolation, boundary) for i in range(n)])
             active = (np.arange(n)[:, None, None] < steps[None]) & hit[None]
             cells = np.where(active[..., None], cells, 0)

@@ -237,6 +237,73 @@ def test_raymarch_signed_extinction(C, bm):
     assert rel((gfull * np.asarray(scale)).sum(-1, keepdims=True), N(rt.grad)) < 1e-4
 
 
+def _ray_direct_and_quad(x, M, V, P, F, shape, bm, blend):
+    """Raymarch forward through the C ABI twice: without a workspace (each block
+    forms its camera, direct gathers) and with one (cameras formed once, quad
+    layout gathers)."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    ops = ngt()
+    attrs = dict(interpolation="LINEAR", boundary=bm, blending_mode=blend, keep_dims=False,
+                 separate_camera_batch=True, emission_scale=None)
+    dev = x.device
+    Mt, Vt, Pt, Ft = (ops._floats(m, w, dev) for m, w in ((M, 16), (V, 16), (P, 16), (F, 6)))
+    outs = []
+    for with_ws in (False, True):
+        out = torch.empty(ops._ray_out_shape(x, Vt, shape, attrs), dtype=torch.float32, device=dev)
+        r = ops._ray_args(x, Mt, Vt, Pt, Ft, shape, out, attrs)
+        ws = None
+        if with_ws:
+            ws = torch.empty(int(L.load().ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))), dtype=torch.uint8,
+                             device=dev)
+            r.workspace, r.workspace_bytes = ops._ptr(ws), ws.numel()
+        L.call("ngt_raymarch_fwd", ctypes.byref(r), ops._stream())
+        torch.cuda.synchronize()
+        outs.append(out)
+    return outs
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
+@pytest.mark.parametrize("blend", BLENDS)
+def test_raymarch_quad_layout(dtype, bm, blend):
+    """One-channel input: the quad-layout gathers equal the direct gathers bit
+    for bit, and forward and exact gradient match the oracle on the stored values."""
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    x32 = (RNG.uniform(0, 1, (1, 10, 12, 14, 1)) * 0.3).astype(np.float32)
+    xt = T(x32, dtype)
+    xs = N(xt.float())
+    direct, quad = _ray_direct_and_quad(xt, M, V, P, F, [10, 8, 6], bm, blend)
+    assert torch.equal(direct, quad)
+    ref = oops.raymarch_grid_transform(xs, M, V, P, F, [10, 8, 6], "LINEAR", bm, blend)
+    assert rel(ref, N(quad)) < 2e-5
+    gy = RNG.standard_normal(ref.shape).astype(np.float32)
+    gx = ngt().raymarch_grid_transform_grad(xt, quad, T(gy), M, V, P, F, [10, 8, 6], "LINEAR", bm, blend,
+                                            grad_mode="exact")
+    rx = oops.raymarch_grid_transform_grad(xs, ref, gy, M, V, P, F, [10, 8, 6], "LINEAR", bm, blend,
+                                           grad_mode="exact")
+    assert rel(rx, N(gx)) < 1e-4
+
+
+@pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
+@pytest.mark.parametrize("dhw", [(1, 5, 6), (7, 1, 4), (5, 6, 1)])
+def test_raymarch_thin_grids(bm, dhw):
+    """Grids one cell thick along an axis (the quad layout's padding then maps
+    both padding coordinates onto the same cell under CLAMP and WRAP)."""
+    M, V, P, F = scene_mats(vol_dhw=dhw, cam_dhw=(10, 8, 6))
+    x = (RNG.uniform(0, 1, (1,) + dhw + (1,)) * 0.5).astype(np.float32)
+    scale = [0.8, 1.1]
+    full = (x * np.asarray(scale, np.float32)).astype(np.float32)
+    xt = T(x).requires_grad_()
+    y = ngt().raymarch_grid_transform(xt, M, V, P, F, [10, 8, 6], boundary=bm, emission_scale=scale)
+    ref = oops.raymarch_grid_transform(full, M, V, P, F, [10, 8, 6], boundary=bm)
+    assert rel(ref, N(y)) < 2e-5
+    gy = RNG.standard_normal(ref.shape).astype(np.float32)
+    y.backward(T(gy))
+    gfull = oops.raymarch_grid_transform_grad(full, ref, gy, M, V, P, F, [10, 8, 6], boundary=bm, grad_mode="exact")
+    assert rel((gfull * np.asarray(scale)).sum(-1, keepdims=True), N(xt.grad)) < 1e-4
+
+
 def test_raymarch_nearest_and_batches():
     M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
     M2 = np.concatenate([M, M])
