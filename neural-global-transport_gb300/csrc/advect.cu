@@ -115,6 +115,8 @@ struct McParams {
   CT<T>* buf;          // reference mode: unnormalised scatter
   unsigned* cnt;       // reference mode: sample counts
   CT<T>* gback;        // deterministic mode: back-trace gradient per cell (gathered afterwards)
+  CT<T>* gface[3];     // density, non-deterministic: face gradients accumulated by backward 2
+  float dt;            // with gface: the lookup is centred(u) * (-dt)
   Dims d;
   int order, clamp, bm, reference;
   int accumulate;      // add (atomically) the direct data gradient instead of writing it
@@ -130,10 +132,9 @@ __device__ __forceinline__ void cell_of(int64_t i, const Dims& d, int& x, int& y
 template <int C, class T, class LK>
 __global__ void __launch_bounds__(kBlock) k_mc_fwd1(McParams<T> p, LK lk) {
   typedef CT<T> S;
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= p.d.count()) return;
   int x, y, z;
-  cell_of(i, p.d, x, y, z);
+  if (!launch_cell(p.d, x, y, z)) return;
+  const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
   S v[C];
@@ -175,10 +176,7 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
   S mn[C], mx[C];
   if (p.clamp == NGT_CLAMP_MC_SMOOTH) {
     const S p1x = add_rn(lut[0], S(x)), p1y = add_rn(lut[1], S(y)), p1z = add_rn(lut[2], S(z));
-    int arg[C];
-    int64_t ci[8];
-    read_extremum<C>(p.data, p1x, p1y, p1z, p.d, p.bm, false, mn, arg, ci);
-    read_extremum<C>(p.data, p1x, p1y, p1z, p.d, p.bm, true, mx, arg, ci);
+    read_minmax<C>(p.data, p1x, p1y, p1z, p.d, p.bm, mn, mx);
   }
 #pragma unroll
   for (int c = 0; c < C; ++c) {
@@ -193,10 +191,9 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
 template <int C, class T, class LK>
 __global__ void __launch_bounds__(kBlock) k_mc_fwd2(McParams<T> p, LK lk) {
   typedef CT<T> S;
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= p.d.count()) return;
   int x, y, z;
-  cell_of(i, p.d, x, y, z);
+  if (!launch_cell(p.d, x, y, z)) return;
+  const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
   McState<C, S> s;
@@ -216,14 +213,19 @@ __device__ __forceinline__ void put_direct(S* p, S v, int accumulate) {
   else *p = v;
 }
 
-// backward 1: gradient of the correction; back-trace adjoint into gfwd
+// backward 1: gradient of the correction; back-trace adjoint into gfwd.  Lanes
+// past the row's end stay in the warp (inactive) for the warp-merged scatter.
 template <int C, class T, class LK>
 __global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
   typedef CT<T> S;
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= p.d.count()) return;
   int x, y, z;
-  cell_of(i, p.d, x, y, z);
+  const bool active = launch_cell(p.d, x, y, z);
+  if (__all_sync(0xffffffffu, !active)) return;
+  if (!active) {  // padding lanes follow the last cell of the row, inactive
+    x = min(x, p.d.x - 1);
+    y = min(y, p.d.y - 1);
+  }
+  const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
   S g[C];
@@ -232,6 +234,7 @@ __global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
     S v[C];
     if (p.clamp == NGT_CLAMP_NEGATIVE)
       read_linear<C>(p.data, add_rn(lut[0], S(x)), add_rn(lut[1], S(y)), add_rn(lut[2], S(z)), p.d, p.bm, v);
+    if (!active) return;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       g[c] = p.gout[i * C + c];
@@ -251,23 +254,29 @@ __global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
       if (p.clamp == NGT_CLAMP_NEGATIVE && !(s.res[c] >= S(0))) g[c] = S(0);
       const S gc = s.mask[c] ? S(0) : g[c];
       gback[c] = -(S(0.5) * gc);
-      put_direct(p.gdata + i * C + c, S(0.5) * gc, p.accumulate);  // direct term of the correction
+      if (active) put_direct(p.gdata + i * C + c, S(0.5) * gc, p.accumulate);  // direct term of the correction
     }
     const S p2x = add_rn(-lut[0], S(x)), p2y = add_rn(-lut[1], S(y)), p2z = add_rn(-lut[2], S(z));
     if (p.det) {
+      if (active) {
 #pragma unroll
-      for (int c = 0; c < C; ++c) {
-        p.gfwd[i * C + c] = g[c];
-        p.gback[i * C + c] = gback[c];
+        for (int c = 0; c < C; ++c) {
+          p.gfwd[i * C + c] = g[c];
+          p.gback[i * C + c] = gback[c];
+        }
       }
     } else if (p.reference) {
+      if (active) {
 #pragma unroll
-      for (int c = 0; c < C; ++c) p.gfwd[i * C + c] = g[c];
-      scatter_linear_counted<C>(p.buf, p.cnt, p2x, p2y, p2z, p.d, p.bm, gback);
+        for (int c = 0; c < C; ++c) p.gfwd[i * C + c] = g[c];
+        scatter_linear_counted<C>(p.buf, p.cnt, p2x, p2y, p2z, p.d, p.bm, gback);
+      }
     } else {
+      if (active) {
 #pragma unroll
-      for (int c = 0; c < C; ++c) atomic_add(p.gfwd + i * C + c, g[c]);
-      scatter_linear<C>(p.gfwd, p2x, p2y, p2z, p.d, p.bm, gback);
+        for (int c = 0; c < C; ++c) atomic_add(p.gfwd + i * C + c, g[c]);
+      }
+      scatter_linear_warp<C>(p.gfwd, p2x, p2y, p2z, p.d, p.bm, gback, active);
     }
     if (!(p.bm == BORDER && !tb.inside)) {
       S dx[C], dy[C], dz[C];
@@ -281,6 +290,7 @@ __global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
       }
     }
   }
+  if (!active) return;
   p.glut[i * 3 + 0] = gl[0];
   p.glut[i * 3 + 1] = gl[1];
   p.glut[i * 3 + 2] = gl[2];
@@ -326,14 +336,20 @@ __global__ void k_norm_add(S* __restrict__ target, S* __restrict__ buf, unsigned
   cnt[i] = 0u;
 }
 
-// backward 2: forward-trace adjoint into the data gradient
+// backward 2: forward-trace adjoint into the data gradient.  With gface set
+// (density lookup centred(u) * (-dt)) the lookup gradient goes straight to the
+// two faces of the cell along each axis (half each, times -dt).
 template <int C, class T, class LK>
 __global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
   typedef CT<T> S;
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= p.d.count()) return;
   int x, y, z;
-  cell_of(i, p.d, x, y, z);
+  const bool active = launch_cell(p.d, x, y, z);
+  if (__all_sync(0xffffffffu, !active)) return;
+  if (!active) {  // padding lanes follow the last cell of the row, inactive
+    x = min(x, p.d.x - 1);
+    y = min(y, p.d.y - 1);
+  }
+  const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
   const S p1x = add_rn(lut[0], S(x)), p1y = add_rn(lut[1], S(y)), p1z = add_rn(lut[2], S(z));
@@ -342,10 +358,11 @@ __global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
   for (int c = 0; c < C; ++c) g[c] = p.gfwd[i * C + c];
   if (p.det) {
   } else if (p.reference) {
-    scatter_linear_counted<C>(p.buf, p.cnt, p1x, p1y, p1z, p.d, p.bm, g);
+    if (active) scatter_linear_counted<C>(p.buf, p.cnt, p1x, p1y, p1z, p.d, p.bm, g);
   } else {
-    scatter_linear<C>(p.gdata, p1x, p1y, p1z, p.d, p.bm, g);
+    scatter_linear_warp<C>(p.gdata, p1x, p1y, p1z, p.d, p.bm, g, active);
   }
+  if (!active) return;
   const Tri<S> t = tri_setup(p1x, p1y, p1z, p.d, p.bm);
   S gl[3] = {p.glut[i * 3 + 0], p.glut[i * 3 + 1], p.glut[i * 3 + 2]};
   if (!(p.bm == BORDER && !t.inside)) {
@@ -359,6 +376,20 @@ __global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
       gl[1] += g[c] * dy[c];
       gl[2] += g[c] * dz[c];
     }
+  }
+  if (p.gface[0]) {
+    const S h = S(-0.5) * S(p.dt);
+    const S gx = gl[0] * h, gy = gl[1] * h, gz = gl[2] * h;
+    S* fx = p.gface[0] + (int64_t(z) * p.d.y + y) * (p.d.x + 1) + x;
+    S* fy = p.gface[1] + (int64_t(z) * (p.d.y + 1) + y) * p.d.x + x;
+    S* fz = p.gface[2] + (int64_t(z) * p.d.y + y) * p.d.x + x;
+    atomic_add(fx, gx);
+    atomic_add(fx + 1, gx);
+    atomic_add(fy, gy);
+    atomic_add(fy + p.d.x, gy);
+    atomic_add(fz, gz);
+    atomic_add(fz + int64_t(p.d.x) * p.d.y, gz);
+    return;
   }
   p.glut[i * 3 + 0] = gl[0];
   p.glut[i * 3 + 1] = gl[1];
@@ -438,6 +469,7 @@ int validate_common(int dtype, const int64_t* dhw, int order, int clamp, int bou
   if (!positive_shape(dhw, 3)) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: shapes must be positive");
   if ((dhw[0] + 1) * (dhw[1] + 1) * (dhw[2] + 1) >= (int64_t(1) << 31))
     return fail(NGT_ERR_INVALID_ARGUMENT, "advect: grid too large");
+  if (dhw[0] + 1 > 65535) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: depth above 65534 cells");
   if (order != 1 && order != 2) return fail(NGT_ERR_INVALID_ARGUMENT, "Unsupported warp order '%d'", order);
   if (clamp < NGT_CLAMP_NONE || clamp > NGT_CLAMP_NEGATIVE) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid clamp");
   if (clamp == NGT_CLAMP_MC_SMOOTH && order != 2) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: MC_SMOOTH needs order 2");
@@ -460,9 +492,9 @@ Dims cells_of(const int64_t* dhw) { return Dims{int(dhw[2]), int(dhw[1]), int(dh
 
 template <int C, class T, class LK>
 void launch_fwd(const McParams<T>& p, const LK& lk, cudaStream_t st) {
-  const unsigned nb = ceil_div_u(p.d.count(), kBlock);
-  k_mc_fwd1<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
-  if (p.order == 2) k_mc_fwd2<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
+  const CellLaunch l = cell_launch(p.d);
+  k_mc_fwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
+  if (p.order == 2) k_mc_fwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
 }
 
 // bwd 1 + 2 of one warp; leaves the lookup gradient in p.glut
@@ -478,11 +510,12 @@ int launch_bwd12(McParams<T>& p, const LK& lk, cudaStream_t st) {
     return check_launch("advect_bwd memset");
   }
   const unsigned nb = ceil_div_u(n, kBlock);
-  k_mc_bwd1<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
+  const CellLaunch l = cell_launch(p.d);
+  k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
   if (p.det && p.order == 2)
     gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st);
   if (p.reference && p.order == 2) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gfwd, p.buf, p.cnt, n);
-  k_mc_bwd2<C, T, LK><<<nb, kBlock, 0, st>>>(p, lk);
+  k_mc_bwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
   if (p.det) gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gfwd, lk, p.d, +1}, n, p.d, p.bm, p.cnt, p.gdata, 1, st);
   if (p.reference) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gdata, p.buf, p.cnt, n);
   return NGT_OK;
@@ -536,9 +569,20 @@ int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
     w += size_t(n) * C * sizeof(S);
     p.cnt = reinterpret_cast<unsigned*>(w);  // gather work area
   }
+  const bool faces = g->vel_x_grad && g->vel_y_grad && g->vel_z_grad;
+  if (faces && !p.det) {
+    // backward 2 accumulates the face gradients itself
+    void* gf[3] = {g->vel_x_grad, g->vel_y_grad, g->vel_z_grad};
+    for (int k = 0; k < 3; ++k) {
+      p.gface[k] = static_cast<S*>(gf[k]);
+      if (cudaMemsetAsync(gf[k], 0, size_t(face_dims(p.d, k).count()) * sizeof(S), st) != cudaSuccess)
+        return check_launch("advect_bwd memset");
+    }
+    p.dt = g->fwd.dt;
+  }
   int rc = launch_bwd12<C, T>(p, centered<T>(&g->fwd), st);
   if (rc) return rc;
-  if (g->vel_x_grad && g->vel_y_grad && g->vel_z_grad) {
+  if (faces && p.det) {
     const Dims& d = p.d;
     const int64_t nf = int64_t(d.x + 1) * d.y * d.z + int64_t(d.x) * (d.y + 1) * d.z + int64_t(d.x) * d.y * (d.z + 1);
     k_centered_faces<S><<<ceil_div_u(nf, kBlock), kBlock, 0, st>>>(p.glut, static_cast<S*>(g->vel_x_grad),

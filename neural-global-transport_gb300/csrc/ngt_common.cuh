@@ -62,6 +62,31 @@ struct Dims {
   __device__ __host__ int64_t count() const { return int64_t(x) * y * z; }
 };
 
+// Cell-parallel launches without integer division: threads (bx, by) over x and
+// y, blockIdx.z over z; bx a multiple of 32, so a warp is 32 consecutive x cells
+// of one row.
+struct CellLaunch {
+  dim3 grid, block;
+};
+
+inline CellLaunch cell_launch(const Dims& d) {
+  const int bx = d.x >= 256 ? 256 : ((d.x + 31) / 32) * 32;
+  int by = 256 / bx;
+  if (by > d.y) by = d.y;
+  CellLaunch l;
+  l.block = dim3(unsigned(bx), unsigned(by), 1);
+  l.grid = dim3(unsigned((d.x + bx - 1) / bx), unsigned((d.y + by - 1) / by), unsigned(d.z));
+  return l;
+}
+
+// This thread's cell of a cell_launch grid; false for padding threads.
+__device__ __forceinline__ bool launch_cell(const Dims& d, int& x, int& y, int& z) {
+  x = int(blockIdx.x * blockDim.x + threadIdx.x);
+  y = int(blockIdx.y * blockDim.y + threadIdx.y);
+  z = int(blockIdx.z);
+  return x < d.x && y < d.y;
+}
+
 __device__ __forceinline__ int64_t flat(int x, int y, int z, const Dims& d) {
   return (int64_t(z) * d.y + y) * d.x + x;
 }
@@ -263,6 +288,100 @@ __device__ __forceinline__ void read_extremum(const T* __restrict__ g, S px, S p
       if (better) {
         out[c] = v;
         arg[c] = k;
+      }
+    }
+  }
+}
+
+// read_extremum's MIN and MAX of the same position in one pass over the corners.
+template <int C, class T, class S>
+__device__ __forceinline__ void read_minmax(const T* __restrict__ g, S px, S py, S pz, const Dims& d, int bm,
+                                           S mn[C], S mx[C]) {
+  const Tri<S> t = tri_setup(px, py, pz, d, bm);
+  bool any_bad = false;
+  bool okk[8];
+  int64_t cidx[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    cidx[k] = tri_corner(t, k, d, okk[k]);
+    any_bad = any_bad || !okk[k];
+  }
+  const bool zero = bm == BORDER && any_bad;
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    mn[c] = zero ? S(0) : S(kFloatMax);
+    mx[c] = zero ? S(0) : S(-kFloatMax);
+  }
+  if (bm == BORDER && !t.inside) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) mn[c] = mx[c] = S(0);
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (!okk[k]) continue;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const S v = S(ld(g + cidx[k] * C + c));
+      if (v < mn[c]) mn[c] = v;
+      if (v > mx[c]) mx[c] = v;
+    }
+  }
+}
+
+// Adjoint of read_linear for a warp whose lanes hold consecutive x cells (all 32
+// lanes call it; ``active`` lanes scatter): when a lane's upper-x corners are the
+// next lane's lower-x corners (same cells, same validity), that lane adds them
+// to its own before the atomics, so neighbouring samples share one atomic per
+// corner.  Same sums as scatter_linear up to the order of the additions.
+template <int C, class S>
+__device__ __forceinline__ void scatter_linear_warp(S* __restrict__ grad, S px, S py, S pz, const Dims& d, int bm,
+                                                    const S g[C], bool active) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const Tri<S> t = tri_setup(px, py, pz, d, bm);
+  const bool on = active && !(bm == BORDER && !t.inside);
+  // corner values: lo[j] at x = i0x, hi[j] at x = i1x, j = (y, z) in reference order
+  S lo[4][C], hi[4][C];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const S wl = tri_weight(t, 2 * j), wh = tri_weight(t, 2 * j + 1);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      lo[j][c] = on ? mul_rn(g[c], wl) : S(0);
+      hi[j][c] = on ? mul_rn(g[c], wh) : S(0);
+    }
+  }
+  // does the previous lane's upper-x column coincide with my lower-x column?
+  const int okyz = int(t.ok0[1]) | (int(t.ok1[1]) << 1) | (int(t.ok0[2]) << 2) | (int(t.ok1[2]) << 3);
+  const int prev_y0 = __shfl_up_sync(full, t.i0[1], 1), prev_y1 = __shfl_up_sync(full, t.i1[1], 1);
+  const int prev_z0 = __shfl_up_sync(full, t.i0[2], 1), prev_z1 = __shfl_up_sync(full, t.i1[2], 1);
+  const int prev_ok = __shfl_up_sync(full, okyz | (int(t.ok1[0]) << 4) | (int(on) << 5), 1);
+  const int prev_x1 = __shfl_up_sync(full, t.i1[0], 1);
+  const bool take = on && lane > 0 && prev_x1 == t.i0[0] && prev_y0 == t.i0[1] && prev_y1 == t.i1[1] &&
+                    prev_z0 == t.i0[2] && prev_z1 == t.i1[2] && prev_ok == (okyz | (int(t.ok0[0]) << 4) | (1 << 5));
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const S r = __shfl_up_sync(full, hi[j][c], 1);
+      if (take) lo[j][c] += r;
+    }
+  const bool given = __shfl_down_sync(full, take, 1) && lane < 31;
+  if (!on) return;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    bool ok;
+    const int64_t il = tri_corner(t, 2 * j, d, ok);
+    if (ok) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) atomic_add(grad + il * C + c, lo[j][c]);
+    }
+    if (!given) {
+      const int64_t ih = tri_corner(t, 2 * j + 1, d, ok);
+      if (ok) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) atomic_add(grad + ih * C + c, hi[j][c]);
       }
     }
   }

@@ -60,14 +60,15 @@ __device__ __forceinline__ uint32_t raw16(T v) {
   return uint32_t(*reinterpret_cast<const uint16_t*>(&v));
 }
 
-// One thread per entry; batch b of N grids at blockIdx.y.
+// One thread per entry, launched as cell_launch over the padded W+1, H+1 and
+// (D+2) * N planes (blockIdx.z = zq + (D+2) * b).
 template <class T>
 __global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename QuadOf<T>::type* __restrict__ q) {
   const QuadDims qd = QuadDims::of(d);
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= qd.count) return;
-  const int b = blockIdx.y;
-  const int xq = int(e % qd.x), yq = int((e / qd.x) % qd.y), zq = int(e / qd.plane);
+  const int xq = int(blockIdx.x * blockDim.x + threadIdx.x), yq = int(blockIdx.y * blockDim.y + threadIdx.y);
+  if (xq >= qd.x || yq >= qd.y) return;
+  const int b = int(blockIdx.z) / qd.z, zq = int(blockIdx.z) - b * qd.z;
+  const int64_t e = (int64_t(zq) * qd.y + yq) * qd.x + xq;
   bool vz;
   const int z = quad_cell(zq - 1, d.z, bm, vz);
   T v[4];
@@ -199,15 +200,16 @@ __device__ __forceinline__ int quad_sources(int i, int n, int bm, int src[3]) {
 }
 
 // Cell gradients from the quad gradient grid, written (not added) to grad; one
-// thread per cell, batch at blockIdx.y.  Component (kx, ky) of entry (xq, yq) is coordinate
+// thread per cell, launched as cell_launch over W, H and D * N planes
+// (blockIdx.z = z + D * b).  Component (kx, ky) of entry (xq, yq) is coordinate
 // (xq - 1 + kx, yq - 1 + ky) of plane zq - 1.
 __global__ void k_quad_fold(const float4* __restrict__ gq, Dims d, int bm, float* __restrict__ grad) {
   const QuadDims qd = QuadDims::of(d);
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= d.count()) return;
-  const int b = blockIdx.y;
+  const int x = int(blockIdx.x * blockDim.x + threadIdx.x), y = int(blockIdx.y * blockDim.y + threadIdx.y);
+  if (x >= d.x || y >= d.y) return;
+  const int b = int(blockIdx.z) / d.z, z = int(blockIdx.z) - b * d.z;
+  const int64_t i = (int64_t(z) * d.y + y) * d.x + x;
   const float4* q = gq + int64_t(b) * qd.count;
-  const int x = int(i % d.x), y = int((i / d.x) % d.y), z = int(i / (int64_t(d.x) * d.y));
   int sx[3], sy[3], sz[3];
   const int nx = quad_sources(x, d.x, bm, sx), ny = quad_sources(y, d.y, bm, sy), nz = quad_sources(z, d.z, bm, sz);
   float acc = 0.0f;

@@ -668,7 +668,7 @@ int64_t slots_of(const ngt_raymarch_args* a) {
 // One-channel LINEAR float / 16-bit inputs are gathered through the quad layout.
 bool quad_case(const ngt_raymarch_args* a) {
   return a->input_shape[4] == 1 && a->interpolation == NGT_LINEAR && a->dtype != NGT_F64 &&
-         a->input_shape[0] <= 65535;
+         a->input_shape[0] * (a->input_shape[1] + 2) <= 65535;
 }
 
 size_t quad_bytes(const ngt_raymarch_args* a) {
@@ -727,18 +727,20 @@ Layout bwd_layout(const ngt_raymarch_grad_args* g) {
 int build_quad(const ngt_raymarch_args* a, void* q, cudaStream_t st) {
   const Dims d = in_dims(a);
   const QuadDims qd = QuadDims::of(d);
-  const dim3 grid(ceil_div_u(qd.count, 256), unsigned(a->input_shape[0]));
+  CellLaunch l = cell_launch(Dims{qd.x, qd.y, qd.z});
+  l.grid.z = unsigned(qd.z * a->input_shape[0]);
+  const dim3 grid = l.grid, blk = l.block;
   switch (a->dtype) {
     case NGT_F32:
-      k_quad_build<float><<<grid, 256, 0, st>>>(static_cast<const float*>(a->input), d, a->boundary,
+      k_quad_build<float><<<grid, blk, 0, st>>>(static_cast<const float*>(a->input), d, a->boundary,
                                                  static_cast<float4*>(q));
       break;
     case NGT_BF16:
-      k_quad_build<__nv_bfloat16><<<grid, 256, 0, st>>>(static_cast<const __nv_bfloat16*>(a->input), d,
+      k_quad_build<__nv_bfloat16><<<grid, blk, 0, st>>>(static_cast<const __nv_bfloat16*>(a->input), d,
                                                          a->boundary, static_cast<uint2*>(q));
       break;
     case NGT_F16:
-      k_quad_build<__half><<<grid, 256, 0, st>>>(static_cast<const __half*>(a->input), d, a->boundary,
+      k_quad_build<__half><<<grid, blk, 0, st>>>(static_cast<const __half*>(a->input), d, a->boundary,
                                                   static_cast<uint2*>(q));
       break;
     default:
@@ -854,9 +856,11 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
     }
     rc = launch_slots(a->fwd.dtype, BWD_EXACT, cin, cb, tiles, st, p);
     if (rc) return rc;
-    if (quad)
-      k_quad_fold<<<dim3(ceil_div_u(vox, 256), unsigned(p.N)), 256, 0, st>>>(p.gquad, p.din, p.bm,
-                                                                            static_cast<float*>(a->input_grad));
+    if (quad) {
+      CellLaunch fl = cell_launch(p.din);
+      fl.grid.z = unsigned(p.din.z * p.N);
+      k_quad_fold<<<fl.grid, fl.block, 0, st>>>(p.gquad, p.din, p.bm, static_cast<float*>(a->input_grad));
+    }
     return check_launch("ngt_raymarch_bwd");
   }
 
