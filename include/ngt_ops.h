@@ -200,6 +200,10 @@ typedef struct {
    * results).  Unused by the backward, which takes its own workspace. */
   void* workspace;
   size_t workspace_bytes;
+  /* Optional: the per-(batch, camera) transforms already formed by
+   * ngt_raymarch_cameras for these matrices (static cameras across calls).
+   * Null: formed on every call.  Used by forward and backward. */
+  const void* cameras;
 } ngt_raymarch_args;
 
 typedef struct {
@@ -218,6 +222,11 @@ typedef struct {
 } ngt_raymarch_grad_args;
 
 size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* args);
+/* Forms the camera block of args' matrices into ``cameras`` (device memory of
+ * ngt_raymarch_cameras_bytes bytes); no counterpart in the reference, whose
+ * launchers upload and invert the matrices per call (raymarch_grid.cu.cc:411-415). */
+size_t ngt_raymarch_cameras_bytes(const ngt_raymarch_args* args);
+int ngt_raymarch_cameras(const ngt_raymarch_args* args, void* cameras, void* stream);
 int ngt_raymarch_fwd(const ngt_raymarch_args* args, void* stream);
 int ngt_raymarch_bwd(const ngt_raymarch_grad_args* args, void* stream);
 size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* args);

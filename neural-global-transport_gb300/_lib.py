@@ -63,7 +63,7 @@ class RaymarchArgs(ctypes.Structure):
                 ("num_cameras", c_i32), ("output", c_vp), ("interpolation", c_i32), ("boundary", c_i32),
                 ("blending_mode", c_i32), ("keep_dims", c_i32), ("separate_camera_batch", c_i32),
                 ("emission_channels", c_i32), ("emission_scale", c_f32 * 4), ("workspace", c_vp),
-                ("workspace_bytes", c_sz)]
+                ("workspace_bytes", c_sz), ("cameras", c_vp)]
 
 
 class RaymarchGradArgs(ctypes.Structure):
@@ -119,6 +119,8 @@ SIGNATURES = {
     "ngt_mip_bytes": ([c_i32, ctypes.POINTER(c_i64), c_i32], c_sz),
     "ngt_lod_transform": ([ctypes.POINTER(LodArgs), c_vp], c_i32),
     "ngt_raymarch_fwd_workspace_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
+    "ngt_raymarch_cameras_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
+    "ngt_raymarch_cameras": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp], c_i32),
     "ngt_raymarch_fwd": ([ctypes.POINTER(RaymarchArgs), c_vp], c_i32),
     "ngt_raymarch_bwd": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
     "ngt_raymarch_bwd_workspace_bytes": ([ctypes.POINTER(RaymarchGradArgs)], c_sz),

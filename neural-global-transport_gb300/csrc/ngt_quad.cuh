@@ -62,8 +62,11 @@ __device__ __forceinline__ uint32_t raw16(T v) {
 
 // One thread per entry, launched as cell_launch over the padded W+1, H+1 and
 // (D+2) * N planes (blockIdx.z = zq + (D+2) * b).
+// With ``neg`` set it also raises *neg when scale * value < 0 for some cell (the
+// extinction-sign check of the raymarch backward).
 template <class T>
-__global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename QuadOf<T>::type* __restrict__ q) {
+__global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename QuadOf<T>::type* __restrict__ q,
+                             int* neg, float scale) {
   const QuadDims qd = QuadDims::of(d);
   const int xq = int(blockIdx.x * blockDim.x + threadIdx.x), yq = int(blockIdx.y * blockDim.y + threadIdx.y);
   if (xq >= qd.x || yq >= qd.y) return;
@@ -79,6 +82,12 @@ __global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename Q
     const int y = quad_cell(yq - 1 + (k >> 1), d.y, bm, vy);
     const T* src = g + int64_t(b) * d.count() + flat(x, y, z, d);
     v[k] = (vx && vy && vz) ? *src : T(0.0f);
+  }
+  if (neg) {
+    bool n = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) n = n || (scale * float(v[k]) < 0.0f);
+    if (__any_sync(__activemask(), n) && n) atomicOr(neg, 1);
   }
   typename QuadOf<T>::type o;
   if constexpr (sizeof(T) == 4) {

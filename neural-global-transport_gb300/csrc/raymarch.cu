@@ -24,6 +24,7 @@ constexpr int kTileX = 16, kTileY = 8, kThreads = kTileX * kTileY;
 constexpr int kSeg = 16;       // exact backward: steps recomputed per segment buffer
 constexpr int kMaxCkpt = 64;   // exact backward: checkpoints per ray
 constexpr int kMaxSteps = 1 << 20;
+constexpr int kMinBlocks = 10;  // forward and one-pass backward: 48 registers, 40 warps per SM
 
 struct RayParams {
   const void* input;
@@ -232,7 +233,7 @@ __global__ void k_build_cams(RayParams p, Cam* __restrict__ cams) {
 
 // ----------------------------------------------------------------- forward
 template <int CIN, int CB, class T, class S>
-__global__ void __launch_bounds__(kThreads) k_raymarch_fwd(RayParams p) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_fwd(RayParams p) {
   __shared__ Cam cam;
   __shared__ CamScratch cam_sh;
   int b, c, oslot;
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
 // extinction channel is checked over the whole grid first (k_extinction_sign),
 // and a launch that can see a negative sample runs k_raymarch_bwd_exact.
 template <int CIN, int CB, class T, class S>
-__global__ void __launch_bounds__(kThreads) k_raymarch_bwd_bl(RayParams p) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(RayParams p) {
   if (*p.flag != 0) return;
   __shared__ Cam cam;
   __shared__ CamScratch cam_sh;
@@ -724,7 +725,7 @@ Layout bwd_layout(const ngt_raymarch_grad_args* g) {
   return l;
 }
 
-int build_quad(const ngt_raymarch_args* a, void* q, cudaStream_t st) {
+int build_quad(const ngt_raymarch_args* a, void* q, cudaStream_t st, int* neg = nullptr, float scale = 1.0f) {
   const Dims d = in_dims(a);
   const QuadDims qd = QuadDims::of(d);
   CellLaunch l = cell_launch(Dims{qd.x, qd.y, qd.z});
@@ -733,15 +734,15 @@ int build_quad(const ngt_raymarch_args* a, void* q, cudaStream_t st) {
   switch (a->dtype) {
     case NGT_F32:
       k_quad_build<float><<<grid, blk, 0, st>>>(static_cast<const float*>(a->input), d, a->boundary,
-                                                 static_cast<float4*>(q));
+                                                 static_cast<float4*>(q), neg, scale);
       break;
     case NGT_BF16:
       k_quad_build<__nv_bfloat16><<<grid, blk, 0, st>>>(static_cast<const __nv_bfloat16*>(a->input), d,
-                                                         a->boundary, static_cast<uint2*>(q));
+                                                         a->boundary, static_cast<uint2*>(q), neg, scale);
       break;
     case NGT_F16:
       k_quad_build<__half><<<grid, blk, 0, st>>>(static_cast<const __half*>(a->input), d, a->boundary,
-                                                  static_cast<uint2*>(q));
+                                                  static_cast<uint2*>(q), neg, scale);
       break;
     default:
       return fail(NGT_ERR_UNSUPPORTED, "raymarch: quad layout needs float or 16-bit storage");
@@ -749,7 +750,12 @@ int build_quad(const ngt_raymarch_args* a, void* q, cudaStream_t st) {
   return NGT_OK;
 }
 
-void build_cams(RayParams& p, void* at, cudaStream_t st) {
+// The call's cameras: the caller's prepared block, else formed into ``at``.
+void build_cams(RayParams& p, const ngt_raymarch_args* a, void* at, cudaStream_t st) {
+  if (a->cameras) {
+    p.cams = static_cast<const Cam*>(a->cameras);
+    return;
+  }
   Cam* cams = static_cast<Cam*>(at);
   k_build_cams<<<unsigned(num_slots(p)), 32, 0, st>>>(p, cams);
   p.cams = cams;
@@ -770,6 +776,18 @@ int launch_slots(int dtype, int which, int cin, int cb, int tiles, cudaStream_t 
 
 using namespace ngt;
 
+extern "C" size_t ngt_raymarch_cameras_bytes(const ngt_raymarch_args* a) { return a ? cams_bytes(a) : 0; }
+
+extern "C" int ngt_raymarch_cameras(const ngt_raymarch_args* a, void* cameras, void* stream) {
+  int cin, cb;
+  const int rc = validate(a, cin, cb);
+  if (rc) return rc;
+  if (!cameras) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_cameras: null output");
+  RayParams p = make_params(a);
+  k_build_cams<<<unsigned(num_slots(p)), 32, 0, as_stream(stream)>>>(p, static_cast<Cam*>(cameras));
+  return check_launch("ngt_raymarch_cameras");
+}
+
 extern "C" size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* a) {
   return a ? fwd_layout(a).total : 0;
 }
@@ -784,12 +802,13 @@ extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null output");
   RayParams p = make_params(a);
   cudaStream_t st = as_stream(stream);
+  if (a->cameras) p.cams = static_cast<const Cam*>(a->cameras);
   if (a->workspace) {
     const Layout l = fwd_layout(a);
     if (a->workspace_bytes < l.total)
       return fail(NGT_ERR_WORKSPACE, "raymarch: the forward workspace needs %zu bytes", l.total);
     char* w = static_cast<char*>(a->workspace);
-    build_cams(p, w + l.cams, st);
+    build_cams(p, a, w + l.cams, st);
     if (quad_case(a)) {
       rc = build_quad(a, w + l.quad, st);
       if (rc) return rc;
@@ -830,12 +849,19 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   const int64_t vox = p.din.count();
   const size_t cs = compute_size(a->fwd.dtype);
   const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
-  build_cams(p, w + l.cams, st);
+  build_cams(p, &a->fwd, w + l.cams, st);
 
   if (a->grad_mode == NGT_GRAD_EXACT) {
     const bool quad = quad_case(&a->fwd);
+    const bool bl = needs_sign_flag(a);
+    if (bl) {
+      p.flag = reinterpret_cast<const int*>(w + l.flag);
+      if (cudaMemsetAsync(w + l.flag, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_bwd memset");
+    }
     if (quad) {
-      rc = build_quad(&a->fwd, w + l.quad, st);
+      // one channel: the quad build also checks the sign of scale * density
+      rc = build_quad(&a->fwd, w + l.quad, st, bl ? reinterpret_cast<int*>(w + l.flag) : nullptr,
+                      cb > 1 ? p.scale[cb - 1] : 1.0f);
       if (rc) return rc;
       p.quad = w + l.quad;
       p.gquad = reinterpret_cast<float4*>(w + l.gquad);
@@ -845,12 +871,11 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
     } else if (cudaMemsetAsync(a->input_grad, 0, size_t(p.N) * vox * cin * cs, st) != cudaSuccess) {
       return check_launch("raymarch_bwd memset");
     }
-    const bool bl = needs_sign_flag(a);
     if (bl) {
-      p.flag = reinterpret_cast<const int*>(w + l.flag);
-      if (cudaMemsetAsync(w + l.flag, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_bwd memset");
-      rc = launch_dtype(a->fwd.dtype, SIGN, cin, cb, dim3(1), st, p);
-      if (rc) return rc;
+      if (!quad) {
+        rc = launch_dtype(a->fwd.dtype, SIGN, cin, cb, dim3(1), st, p);
+        if (rc) return rc;
+      }
       rc = launch_slots(a->fwd.dtype, BWD_BL, cin, cb, tiles, st, p);
       if (rc) return rc;
     }

@@ -23,10 +23,10 @@ from .ops import _code, _ptr
 
 
 class RenderAdvectStep:
-    # kernels of one f32 exact Beer-Lambert step: advect fwd 2, raymarch fwd 3 (cameras,
-    # quad layout, march), loss 1, raymarch bwd 6 (cameras, quad layout, sign check,
-    # one-pass and checkpointed marches, fold), advect bwd 3
-    KERNELS_PER_STEP = 15
+    # kernels of one f32 exact Beer-Lambert step: advect fwd 2, raymarch fwd 2 (quad
+    # layout, march), loss 1, raymarch bwd 4 (quad layout with the sign check,
+    # one-pass and checkpointed marches, fold), advect bwd 2
+    KERNELS_PER_STEP = 11
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact"):
@@ -91,6 +91,12 @@ class RenderAdvectStep:
         self.ray_fws = torch.empty(int(self.lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))),
                                    dtype=torch.uint8, device=dev)
         r.workspace, r.workspace_bytes = _ptr(self.ray_fws), self.ray_fws.numel()
+        # the cameras are fixed for the optimisation: their transforms are formed once
+        self.cameras = torch.empty(int(self.lib.ngt_raymarch_cameras_bytes(ctypes.byref(r))), dtype=torch.uint8,
+                                   device=dev)
+        self._call("ngt_raymarch_cameras", ctypes.byref(r), _ptr(self.cameras),
+                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        r.cameras = _ptr(self.cameras)
         self.ray = r
         rg = L.RaymarchGradArgs()
         rg.fwd = r
