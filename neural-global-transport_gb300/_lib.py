@@ -124,6 +124,7 @@ SIGNATURES = {
     "ngt_raymarch_fwd": ([ctypes.POINTER(RaymarchArgs), c_vp], c_i32),
     "ngt_raymarch_bwd": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
     "ngt_raymarch_bwd_workspace_bytes": ([ctypes.POINTER(RaymarchGradArgs)], c_sz),
+    "ngt_raymarch_bwd_static": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
     "ngt_reduce_blend_fwd": ([ctypes.POINTER(ReduceBlendArgs), c_vp], c_i32),
     "ngt_reduce_blend_bwd": ([ctypes.POINTER(ReduceBlendGradArgs), c_vp], c_i32),
     "ngt_advect_maccormack_fwd": ([ctypes.POINTER(AdvectArgs), c_vp], c_i32),

@@ -17,6 +17,8 @@
 #include "ngt_blend.cuh"
 #include "ngt_quad.cuh"
 
+#include <mutex>
+
 namespace ngt {
 namespace {
 
@@ -915,4 +917,57 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
     }
   }
   return check_launch("ngt_raymarch_bwd");
+}
+
+// ------------------------------------------ backward without caller memory
+// For callers that cannot allocate device memory: the backward's scratch
+// (sign flag, cameras, quad layout and quad gradient) lives in one file-scope
+// device array of kStaticScratchBytes.  Every call shares it; what must start
+// at zero (the sign flag, the quad gradient, the reference-mode buffers) is
+// cleared inside each call by ngt_raymarch_bwd's own stream-ordered memsets.
+// Calls whose work overlaps on the GPU (other streams, other host threads)
+// race on the array.
+namespace ngt {
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;
+constexpr int kMaxDevices = 64;
+__device__ __align__(256) unsigned char g_raymarch_scratch[kStaticScratchBytes];
+
+std::mutex g_scratch_mutex;
+void* g_scratch_ptr[kMaxDevices] = {};
+
+// The array's device address on the current device, looked up once per device.
+int scratch_address(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("raymarch_bwd_static: cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(NGT_ERR_UNSUPPORTED, "raymarch_bwd_static: device %d", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_raymarch_scratch);
+    if (e != cudaSuccess)
+      return fail(NGT_ERR_CUDA, "raymarch_bwd_static: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return NGT_OK;
+}
+
+}  // namespace
+}  // namespace ngt
+
+extern "C" int ngt_raymarch_bwd_static(const ngt_raymarch_grad_args* a, void* stream) {
+  if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd_static: null arguments");
+  const size_t need = bwd_layout(a).total;
+  if (need > kStaticScratchBytes)
+    return fail(NGT_ERR_WORKSPACE, "raymarch_bwd_static: this call needs %zu scratch bytes, above the %zu-byte static scratch",
+                need, kStaticScratchBytes);
+  void* scratch = nullptr;
+  const int rc = scratch_address(&scratch);
+  if (rc) return rc;
+  ngt_raymarch_grad_args b = *a;
+  b.workspace = scratch;
+  b.workspace_bytes = kStaticScratchBytes;
+  return ngt_raymarch_bwd(&b, stream);
 }
