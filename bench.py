@@ -124,6 +124,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+# DRAM bytes (read + write) per call of the dominant library call, summed over its
+# kernels, from one ncu capture of this workload in f32 (cold cache per kernel):
+# profiles/step_f32_128cube_5views_kernels.md
+NCU_TRAFFIC_F32 = {"raymarch_bwd": 116.27e6}
+
+
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -301,7 +307,8 @@ def gpu_arm(args, world, rank, local):
         name, avg_ms, nbytes = kernel
         achieved = nbytes / (avg_ms * 1e-3) / 1e9
         line["roofline"] = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                            "frac": achieved / peak, "peak_kind": peak_kind,
+                            "traffic": NCU_TRAFFIC_F32.get(name) if args.dtype == "f32" else None,
                             "algorithmic_bytes_per_launch": nbytes, "avg_ms": avg_ms}
     if clk:
         line["clocks"] = clk
