@@ -48,6 +48,36 @@ def config1_small():
     return render_step(grid=(64, 64, 64), views=1, image=(128, 128), depth=64, max_u=1.0)
 
 
+def plume_chain(grid=(96, 176, 96), frames=120, image=(192, 192), depth=96, up=0.5, noise=0.3, source_sigma=6.0,
+                source_amp=0.1, density_seed=0, velocity_seed=5, target_seed=2, target_noise=0.05):
+    """The long chain: a plume-aspect grid (D, H, W), inflow source near the bottom
+    (y = 8) added every frame, velocity (0, +up, 0) cells/step plus curl noise of
+    max ``noise``, one front camera.  The initial density is three blobs in the
+    lower half; the targets come from the same chain started from the blobs with
+    amplitudes perturbed by ``target_noise`` (rendered by the caller)."""
+    D, H, W = grid
+    lo = np.array([W * 0.3, H * 0.1, D * 0.3])
+    hi = np.array([W * 0.7, H * 0.45, D * 0.7])
+    sig = (min(grid) / 16.0, min(grid) / 8.0)
+    rho0 = synthetic.gaussian_blobs(grid, n=3, center_lo=lo, center_hi=hi, sigma=sig, seed=density_seed)
+    rho0_target = synthetic.gaussian_blobs(grid, n=3, center_lo=lo, center_hi=hi, sigma=sig, seed=density_seed,
+                                           amp_noise=target_noise, noise_seed=target_seed)
+    ux, uy, uz = synthetic.plume_velocity(grid, up=up, noise=noise, seed=velocity_seed)
+    src = synthetic.inflow_source(grid, sigma=source_sigma, amplitude=source_amp, height=min(8.0, H / 4))
+    cams = scene.orbit_cameras([depth, image[0], image[1]], [0.0])
+    vol = scene.volume_transform(list(grid))
+    M = scene.model_params([vol])
+    V, P, F = scene.camera_params(cams)
+    return Workload(rho0=rho0, rho0_target=rho0_target, ux=ux, uy=uy, uz=uz, source=src, M=M, V=V, P=P, F=F,
+                    cameras=cams, image_dhw=(depth, image[0], image[1]), grid=tuple(grid), frames=frames,
+                    depth_step=cams[0].depth_step)
+
+
+def config3():
+    """96 x 176 x 96 plume, 120 frames, one 192 x 192 x 96 camera."""
+    return plume_chain()
+
+
 def algorithmic_bytes(grid, views, image, elem=4):
     """Compulsory HBM bytes of one differentiated step: every tensor that must
     cross HBM counted once at its storage size (density read / advected write /
