@@ -41,6 +41,10 @@ def parse():
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--cpu-baseline", default="on", choices=["on", "off"])
     ap.add_argument("--kernel-stats", default="on", choices=["on", "off"])
+    ap.add_argument("--workload", default="step", choices=["step", "chain", "large"],
+                    help="step: the headline differentiated step; chain: the checkpointed 120-frame plume "
+                         "chain; large: 256x448x256 grid, 8 views at 512x512x256, 16-bit storage errors")
+    ap.add_argument("--checkpoint-every", type=int, default=10)
     return ap.parse_args()
 
 
@@ -395,11 +399,132 @@ def e2e_measure(torch, dev, w, st, tgt, args, flush):
             "path": "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + torch loss.backward()"}
 
 
+# ------------------------------------------------------------ other workloads
+def _timed(torch, fn, steps, warmup, flush):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    stream = torch.cuda.current_stream()
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        fn()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return float(np.mean([a.elapsed_time(b) for a, b in ev]))
+
+
+def chain_arm(args, local):
+    """The checkpointed multi-frame chain (96x176x96 plume, 120 frames, one
+    192x192x96 camera): forward with checkpoints every K frames, backward with
+    per-segment recompute, as one CUDA graph."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from ngt_gb300 import _build, workloads
+    from ngt_gb300.chain import AdvectRenderChain, chain_targets
+    _build.build_library()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workloads.config3()
+    st = {"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[args.dtype]
+    T = lambda a: torch.as_tensor(a, device=dev).to(st).contiguous()
+    u = [T(w.ux), T(w.uy), T(w.uz)]
+    tg = chain_targets(T(w.rho0_target), *u, T(w.source), w.M, w.V, w.P, w.F, w.image_dhw, w.frames)
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    ch = AdvectRenderChain(T(w.rho0), *u, T(w.source), w.M, w.V, w.P, w.F, tg, w.image_dhw, w.frames,
+                           checkpoint_every=args.checkpoint_every)
+    ch.capture()
+    chain_bytes = torch.cuda.max_memory_allocated() - base
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    ms = _timed(torch, ch.run, args.steps, max(args.warmup, 3), flush)
+    D, H, W = w.grid
+    line = {"metric": "checkpointed plume chain fwd+bwd frames/s", "value": w.frames * 1e3 / ms,
+            "unit": "frames/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_chain": ms, "higher_is_better": True, "dtype": args.dtype, "data": "synthetic plume",
+            "config": {"workload": "MacCormack + 1-view render per frame, %d frames, checkpoint every %d" %
+                                   (w.frames, args.checkpoint_every),
+                       "grid": [D, H, W], "image": list(w.image_dhw[1:]), "depth_samples": w.image_dhw[0],
+                       "l2": "flushed between timed chains", "cuda_graph": True},
+            "loss": float(ch.loss.item()), "chain_device_bytes": int(chain_bytes),
+            "stored_densities": ch.nseg + ch.K + 3, "densities_without_checkpoints": 2 * w.frames}
+    print(json.dumps(line), flush=True)
+
+
+def large_arm(args, local):
+    """The reduced-precision configuration: 256x448x256 density and MAC velocity,
+    8 views at 512x512 with 256 depth samples; the step in FP32 and in 16-bit
+    storage, and the errors of every image and gradient against the FP64 path."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from ngt_gb300 import _build, ops, workloads
+    from ngt_gb300.step import RenderAdvectStep
+    _build.build_library()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workloads.render_step(grid=(256, 448, 256), views=8, image=(512, 512), depth=256, max_u=2.0)
+    with torch.no_grad():
+        tgt = ops.raymarch_grid_transform(torch.as_tensor(w.rho_target, device=dev, dtype=torch.float64)[None],
+                                          w.M, w.V, w.P, w.F, w.image_dhw,
+                                          emission_scale=(w.depth_step, w.depth_step))[..., :1]
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def make(dt, inputs=None):
+        a = inputs or (w.rho, w.ux, w.uy, w.uz)
+        t = [torch.as_tensor(x, device=dev).to(dt).contiguous() for x in a]
+        return RenderAdvectStep(*t, w.M, w.V, w.P, w.F, tgt, w.image_dhw)
+
+    results = {}
+    ref = make(torch.float64)
+    ref.step()
+    torch.cuda.synchronize()
+    ref_out = [ref.image.clone()] + [g.clone() for g in ref.gradients()]
+    del ref
+    names = ["image", "d_rho", "d_ux", "d_uy", "d_uz"]
+    f32_out = None
+    for name, dt in (("f32", torch.float32), ("bf16", torch.bfloat16), ("f16", torch.float16)):
+        s = make(dt)
+        s.capture()
+        ms = _timed(torch, s.step, args.steps, max(args.warmup, 3), flush)
+        out = [s.image.clone()] + [g.clone() for g in s.gradients()]
+        errs = {}
+        for n, a, b in zip(names, out, ref_out):
+            a, b = a.double(), b.double()
+            errs[n] = {"rel_l2_vs_fp64": float((a - b).norm() / b.norm()),
+                       "max_abs_vs_fp64": float((a - b).abs().max())}
+            if f32_out is not None:
+                c = f32_out[names.index(n)].double()
+                errs[n]["rel_l2_vs_fp32"] = float((a - c).norm() / c.norm())
+        if name == "f32":
+            f32_out = out
+        results[name] = {"ms_per_step": ms, "errors": errs}
+        del s
+        torch.cuda.empty_cache()
+    line = {"metric": "fwd+bwd render+advect steps/s at 256x448x256 x 8 views (16-bit storage)",
+            "value": 1e3 / results["bf16"]["ms_per_step"], "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "higher_is_better": True, "dtype": "bf16 storage, f32 arithmetic",
+            "data": "synthetic (seeded Gaussian blobs, curl-noise MAC velocity)",
+            "config": {"workload": "MacCormack + 8-view Beer-Lambert raymarch 512x512x256 + L2 + backward",
+                       "grid": [256, 448, 256], "views": 8, "image": [512, 512], "depth_samples": 256,
+                       "l2": "flushed between timed steps"},
+            "bf16_speedup_vs_f32": results["f32"]["ms_per_step"] / results["bf16"]["ms_per_step"],
+            "f16_speedup_vs_f32": results["f32"]["ms_per_step"] / results["f16"]["ms_per_step"],
+            "runs": results}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_init(args)
     if args.impl == "reference":
         reference_arm(args, world, rank)
+    elif args.workload == "chain":
+        chain_arm(args, local)
+    elif args.workload == "large":
+        large_arm(args, local)
     else:
         gpu_arm(args, world, rank, local)
     if world > 1:

@@ -214,3 +214,21 @@ class AdvectRenderChain:
     def gradients(self):
         """(d loss / d rho_0, d loss / d u_x, u_y, u_z)."""
         return (self.g_rho[self.result],) + tuple(self.g_u)
+
+
+def chain_targets(rho0, ux, uy, uz, source, M, V, P, F, image_dhw, frames, dt=1.0, light=1.0,
+                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER"):
+    """Target images of a chain: the light channel of every frame's render,
+    (frames, views, H, W, 1), through the operator API."""
+    from . import advect, ops
+    F32 = torch.as_tensor(F, dtype=torch.float32).reshape(-1, 6)
+    step = float(F32[0, 1] - F32[0, 0]) / image_dhw[0]
+    out = []
+    rho = rho0
+    with torch.no_grad():
+        for _ in range(frames):
+            rho = advect.warp(rho, ux, uy, uz, dt=dt, order=2, clamp=clamp, boundary=advect_boundary) + source
+            img = ops.raymarch_grid_transform(rho[None], M, V, P, F, image_dhw, boundary=render_boundary,
+                                              emission_scale=(light * step, step))
+            out.append(img[0, ..., :1])
+    return torch.stack(out)
