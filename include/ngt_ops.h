@@ -341,6 +341,34 @@ int ngt_advect_velocity_fwd(const ngt_advect_velocity_args* args, void* stream);
 int ngt_advect_velocity_bwd(const ngt_advect_velocity_grad_args* args, void* stream);
 size_t ngt_advect_velocity_bwd_workspace_bytes(const ngt_advect_velocity_grad_args* args);
 
+/* ------------------------------------------------------------------ batches */
+/* Many scenes of different grid, image and depth sizes per call (no
+ * counterpart in the reference, whose ops take one grid shape per call and are
+ * called once per scene).  Each scene's arguments are those of the single-scene
+ * call; up to 32 scenes, sharing dtype and channel layout.
+ *
+ * Raymarch: one persistent launch per pass; blocks take (scene, camera, 16x8
+ * ray tile) work items from a counter, largest scenes first.  ``blocks_per_sm``
+ * sets the persistent grid (0: default), the knob an autotuner sets.  Workspace
+ * from ngt_raymarch_batch_workspace_bytes (work counters, per-scene flags, the
+ * cameras of scenes without a prepared ``cameras`` block).  The backward takes
+ * exact Beer-Lambert gradients of LINEAR sampling (one-pass for scenes with
+ * non-negative extinction, checkpointed otherwise); input gradients are float. */
+size_t ngt_raymarch_batch_workspace_bytes(const ngt_raymarch_args* scenes, int32_t count);
+int ngt_raymarch_fwd_batch(const ngt_raymarch_args* scenes, int32_t count, int32_t blocks_per_sm, void* workspace,
+                           size_t workspace_bytes, void* stream);
+int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* scenes, int32_t count, int32_t blocks_per_sm,
+                           void* workspace, size_t workspace_bytes, void* stream);
+
+/* Density warps of many grids: one launch per phase over the concatenated z
+ * planes.  The backward takes exact, non-deterministic gradients with all three
+ * face gradients; workspace from ngt_advect_maccormack_bwd_batch_workspace_bytes
+ * (args' own workspace fields are ignored). */
+int ngt_advect_maccormack_fwd_batch(const ngt_advect_args* grids, int32_t count, void* stream);
+size_t ngt_advect_maccormack_bwd_batch_workspace_bytes(const ngt_advect_grad_args* grids, int32_t count);
+int ngt_advect_maccormack_bwd_batch(const ngt_advect_grad_args* grids, int32_t count, void* workspace,
+                                    size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------ step helpers */
 /* Image loss of the reconstruction step, 0.5 * sum over pixels of
  * (image[..., c] - target[..., c])^2 for the first ``loss_channels`` channels

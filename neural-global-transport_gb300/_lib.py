@@ -125,6 +125,12 @@ SIGNATURES = {
     "ngt_raymarch_bwd": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
     "ngt_raymarch_bwd_workspace_bytes": ([ctypes.POINTER(RaymarchGradArgs)], c_sz),
     "ngt_raymarch_bwd_static": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
+    "ngt_raymarch_batch_workspace_bytes": ([ctypes.POINTER(RaymarchArgs), c_i32], c_sz),
+    "ngt_raymarch_fwd_batch": ([ctypes.POINTER(RaymarchArgs), c_i32, c_i32, c_vp, c_sz, c_vp], c_i32),
+    "ngt_raymarch_bwd_batch": ([ctypes.POINTER(RaymarchGradArgs), c_i32, c_i32, c_vp, c_sz, c_vp], c_i32),
+    "ngt_advect_maccormack_fwd_batch": ([ctypes.POINTER(AdvectArgs), c_i32, c_vp], c_i32),
+    "ngt_advect_maccormack_bwd_batch_workspace_bytes": ([ctypes.POINTER(AdvectGradArgs), c_i32], c_sz),
+    "ngt_advect_maccormack_bwd_batch": ([ctypes.POINTER(AdvectGradArgs), c_i32, c_vp, c_sz, c_vp], c_i32),
     "ngt_reduce_blend_fwd": ([ctypes.POINTER(ReduceBlendArgs), c_vp], c_i32),
     "ngt_reduce_blend_bwd": ([ctypes.POINTER(ReduceBlendGradArgs), c_vp], c_i32),
     "ngt_advect_maccormack_fwd": ([ctypes.POINTER(AdvectArgs), c_vp], c_i32),

@@ -130,10 +130,8 @@ __device__ __forceinline__ void cell_of(int64_t i, const Dims& d, int& x, int& y
 }
 
 template <int C, class T, class LK>
-__global__ void __launch_bounds__(kBlock) k_mc_fwd1(McParams<T> p, LK lk) {
+__device__ __forceinline__ void mc_fwd1_at(const McParams<T>& p, const LK& lk, int x, int y, int z) {
   typedef CT<T> S;
-  int x, y, z;
-  if (!launch_cell(p.d, x, y, z)) return;
   const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
@@ -149,6 +147,13 @@ __global__ void __launch_bounds__(kBlock) k_mc_fwd1(McParams<T> p, LK lk) {
 #pragma unroll
     for (int c = 0; c < C; ++c) p.fwd[i * C + c] = v[c];
   }
+}
+
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_fwd1(McParams<T> p, LK lk) {
+  int x, y, z;
+  if (!launch_cell(p.d, x, y, z)) return;
+  mc_fwd1_at<C>(p, lk, x, y, z);
 }
 
 template <int C, class S>
@@ -189,10 +194,8 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
 }
 
 template <int C, class T, class LK>
-__global__ void __launch_bounds__(kBlock) k_mc_fwd2(McParams<T> p, LK lk) {
+__device__ __forceinline__ void mc_fwd2_at(const McParams<T>& p, const LK& lk, int x, int y, int z) {
   typedef CT<T> S;
-  int x, y, z;
-  if (!launch_cell(p.d, x, y, z)) return;
   const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
@@ -207,6 +210,13 @@ __global__ void __launch_bounds__(kBlock) k_mc_fwd2(McParams<T> p, LK lk) {
   }
 }
 
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_fwd2(McParams<T> p, LK lk) {
+  int x, y, z;
+  if (!launch_cell(p.d, x, y, z)) return;
+  mc_fwd2_at<C>(p, lk, x, y, z);
+}
+
 template <class S>
 __device__ __forceinline__ void put_direct(S* p, S v, int accumulate) {
   if (accumulate) atomic_add(p, v);
@@ -215,17 +225,25 @@ __device__ __forceinline__ void put_direct(S* p, S v, int accumulate) {
 
 // backward 1: gradient of the correction; back-trace adjoint into gfwd.  Lanes
 // past the row's end stay in the warp (inactive) for the warp-merged scatter.
+// (x, y, z) is a cell of the grid; inactive lanes (padding, clamped onto the
+// row's last cell) take part in the warp-merged scatter only.
 template <int C, class T, class LK>
-__global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
+__device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, int x, int y, int z, bool active) {
   typedef CT<T> S;
-  int x, y, z;
-  const bool active = launch_cell(p.d, x, y, z);
-  if (__all_sync(0xffffffffu, !active)) return;
-  if (!active) {  // padding lanes follow the last cell of the row, inactive
-    x = min(x, p.d.x - 1);
-    y = min(y, p.d.y - 1);
-  }
   const int64_t i = flat(x, y, z, p.d);
+  if (p.gface[0] && active) {
+    // clear the face gradients that backward 2 accumulates: each cell its lower
+    // face per axis, the last cell of a line also the upper one
+    S* fx = p.gface[0] + (int64_t(z) * p.d.y + y) * (p.d.x + 1) + x;
+    S* fy = p.gface[1] + (int64_t(z) * (p.d.y + 1) + y) * p.d.x + x;
+    S* fz = p.gface[2] + (int64_t(z) * p.d.y + y) * p.d.x + x;
+    fx[0] = S(0);
+    fy[0] = S(0);
+    fz[0] = S(0);
+    if (x == p.d.x - 1) fx[1] = S(0);
+    if (y == p.d.y - 1) fy[p.d.x] = S(0);
+    if (z == p.d.z - 1) fz[int64_t(p.d.x) * p.d.y] = S(0);
+  }
   S lut[3];
   lk(x, y, z, lut);
   S g[C];
@@ -296,6 +314,18 @@ __global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
   p.glut[i * 3 + 2] = gl[2];
 }
 
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
+  int x, y, z;
+  const bool active = launch_cell(p.d, x, y, z);
+  if (__all_sync(0xffffffffu, !active)) return;
+  if (!active) {  // padding lanes follow the last cell of the row, inactive
+    x = min(x, p.d.x - 1);
+    y = min(y, p.d.y - 1);
+  }
+  mc_bwd1_at<C>(p, lk, x, y, z, active);
+}
+
 // gather sources of the deterministic form: the back-trace (value gback at
 // idx - lut) and the forward trace (value gfwd at idx + lut)
 template <int C, class T, class LK>
@@ -339,16 +369,11 @@ __global__ void k_norm_add(S* __restrict__ target, S* __restrict__ buf, unsigned
 // backward 2: forward-trace adjoint into the data gradient.  With gface set
 // (density lookup centred(u) * (-dt)) the lookup gradient goes straight to the
 // two faces of the cell along each axis (half each, times -dt).
+// (x, y, z) is a cell of the grid; inactive lanes (padding, clamped onto the
+// row's last cell) take part in the warp-merged scatter only.
 template <int C, class T, class LK>
-__global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
+__device__ __forceinline__ void mc_bwd2_at(const McParams<T>& p, const LK& lk, int x, int y, int z, bool active) {
   typedef CT<T> S;
-  int x, y, z;
-  const bool active = launch_cell(p.d, x, y, z);
-  if (__all_sync(0xffffffffu, !active)) return;
-  if (!active) {  // padding lanes follow the last cell of the row, inactive
-    x = min(x, p.d.x - 1);
-    y = min(y, p.d.y - 1);
-  }
   const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
@@ -394,6 +419,18 @@ __global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
   p.glut[i * 3 + 0] = gl[0];
   p.glut[i * 3 + 1] = gl[1];
   p.glut[i * 3 + 2] = gl[2];
+}
+
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
+  int x, y, z;
+  const bool active = launch_cell(p.d, x, y, z);
+  if (__all_sync(0xffffffffu, !active)) return;
+  if (!active) {  // padding lanes follow the last cell of the row, inactive
+    x = min(x, p.d.x - 1);
+    y = min(y, p.d.y - 1);
+  }
+  mc_bwd2_at<C>(p, lk, x, y, z, active);
 }
 
 // density backward 3: d u_c = -dt * d lut; each face receives half of its two cells
@@ -459,6 +496,46 @@ __global__ void __launch_bounds__(kBlock) k_face_lut_adjoint(const S* __restrict
         scatter_linear<1>(gu[s], px, py, pz, face_dims(cells, s), bm, gg);
       }
     }
+  }
+}
+
+// ---------------------------------------------------- batched density warps
+// Many grids of different sizes in one launch per phase: blockIdx.z runs over
+// the concatenated z planes of all grids, blockIdx.x / y over the largest grid's
+// rows (threads outside a grid's x / y extent are padding).
+constexpr int kMaxAdvBatch = 32;
+
+template <class T, class LK>
+struct McBatch {
+  McParams<T> item[kMaxAdvBatch];
+  LK lk[kMaxAdvBatch];
+  int z_end[kMaxAdvBatch];  // cumulative z planes
+  int count;
+};
+
+template <int C, class T, class LK, int PHASE>
+__global__ void __launch_bounds__(kBlock) k_mc_batch(const __grid_constant__ McBatch<T, LK> bb) {
+  int it = 0;
+  const int zz = int(blockIdx.z);
+  while (it < bb.count - 1 && bb.z_end[it] <= zz) ++it;
+  const McParams<T>& p = bb.item[it];
+  const int z = zz - (it ? bb.z_end[it - 1] : 0);
+  int x = int(blockIdx.x * blockDim.x + threadIdx.x), y = int(blockIdx.y * blockDim.y + threadIdx.y);
+  const bool active = x < p.d.x && y < p.d.y;
+  if (PHASE == 0) {
+    if (active) mc_fwd1_at<C>(p, bb.lk[it], x, y, z);
+  } else if (PHASE == 1) {
+    if (active && p.order == 2) mc_fwd2_at<C>(p, bb.lk[it], x, y, z);
+  } else {
+    if (__all_sync(0xffffffffu, !active)) return;
+    if (!active) {
+      x = min(x, p.d.x - 1);
+      y = min(y, p.d.y - 1);
+    }
+    if (PHASE == 2)
+      mc_bwd1_at<C>(p, bb.lk[it], x, y, z, active);
+    else
+      mc_bwd2_at<C>(p, bb.lk[it], x, y, z, active);
   }
 }
 
@@ -571,13 +648,10 @@ int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
   }
   const bool faces = g->vel_x_grad && g->vel_y_grad && g->vel_z_grad;
   if (faces && !p.det) {
-    // backward 2 accumulates the face gradients itself
-    void* gf[3] = {g->vel_x_grad, g->vel_y_grad, g->vel_z_grad};
-    for (int k = 0; k < 3; ++k) {
-      p.gface[k] = static_cast<S*>(gf[k]);
-      if (cudaMemsetAsync(gf[k], 0, size_t(face_dims(p.d, k).count()) * sizeof(S), st) != cudaSuccess)
-        return check_launch("advect_bwd memset");
-    }
+    // backward 1 clears the face gradients, backward 2 accumulates them
+    p.gface[0] = static_cast<S*>(g->vel_x_grad);
+    p.gface[1] = static_cast<S*>(g->vel_y_grad);
+    p.gface[2] = static_cast<S*>(g->vel_z_grad);
     p.dt = g->fwd.dt;
   }
   int rc = launch_bwd12<C, T>(p, centered<T>(&g->fwd), st);
@@ -724,6 +798,115 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
 template <class F>
 int by_dtype(int dtype, F&& f);
 
+// ------------------------------------------------------------ batched warps
+int validate_batch(const ngt_advect_args* const* a, int count, int& zsum, int& maxw, int& maxh) {
+  if (count < 1 || count > kMaxAdvBatch)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: 1 to %d grids", kMaxAdvBatch);
+  zsum = maxw = maxh = 0;
+  for (int i = 0; i < count; ++i) {
+    const int rc = validate(a[i]);
+    if (rc) return rc;
+    if (!a[i]->output) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null output");
+    if (a[i]->dtype != a[0]->dtype || a[i]->channels != a[0]->channels)
+      return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: grids must share dtype and channels");
+    zsum += int(a[i]->grid_dhw[0]);
+    maxw = max(maxw, int(a[i]->grid_dhw[2]));
+    maxh = max(maxh, int(a[i]->grid_dhw[1]));
+  }
+  if (zsum > 65535) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: more than 65535 z planes in total");
+  return NGT_OK;
+}
+
+dim3 batch_grid(int maxw, int maxh, int zsum) {
+  return dim3(unsigned((maxw + 31) / 32), unsigned((maxh + 7) / 8), unsigned(zsum));
+}
+
+template <int C, class T>
+int density_fwd_batch(const ngt_advect_args* const* a, int count, int zsum, int maxw, int maxh, cudaStream_t st) {
+  McBatch<T, CenteredLookup<T>> bb{};
+  bb.count = count;
+  int z = 0;
+  bool mc = false;
+  for (int k = 0; k < count; ++k) {
+    bb.item[k] = density_params<T>(a[k]);
+    bb.lk[k] = centered<T>(a[k]);
+    z += int(a[k]->grid_dhw[0]);
+    bb.z_end[k] = z;
+    mc = mc || a[k]->order == 2;
+  }
+  const dim3 grid = batch_grid(maxw, maxh, zsum), block(32, 8);
+  k_mc_batch<C, T, CenteredLookup<T>, 0><<<grid, block, 0, st>>>(bb);
+  if (mc) k_mc_batch<C, T, CenteredLookup<T>, 1><<<grid, block, 0, st>>>(bb);
+  return check_launch("ngt_advect_maccormack_fwd_batch");
+}
+
+// Workspace of a batched backward: [gfwd of every grid][glut of every grid].
+size_t batch_bwd_bytes(const ngt_advect_grad_args* g, int count) {
+  size_t n = 0, m = 0;
+  for (int k = 0; k < count; ++k) {
+    const int64_t cells = g[k].fwd.grid_dhw[0] * g[k].fwd.grid_dhw[1] * g[k].fwd.grid_dhw[2];
+    const size_t cs = compute_size(g[k].fwd.dtype);
+    n += size_t(cells) * size_t(g[k].fwd.channels) * cs;
+    m += size_t(cells) * 3 * cs;
+  }
+  return n + m;
+}
+
+template <int C, class T>
+int density_bwd_batch(const ngt_advect_grad_args* g, int count, int zsum, int maxw, int maxh, void* ws,
+                      cudaStream_t st) {
+  typedef CT<T> S;
+  McBatch<T, CenteredLookup<T>> bb{};
+  bb.count = count;
+  size_t gfwd_bytes = 0;
+  for (int k = 0; k < count; ++k)
+    gfwd_bytes += size_t(g[k].fwd.grid_dhw[0] * g[k].fwd.grid_dhw[1] * g[k].fwd.grid_dhw[2]) * C * sizeof(S);
+  char* wf = static_cast<char*>(ws);
+  char* wl = wf + gfwd_bytes;
+  int z = 0;
+  for (int k = 0; k < count; ++k) {
+    McParams<T> p = density_params<T>(&g[k].fwd);
+    const int64_t n = p.d.count();
+    p.gout = static_cast<const S*>(g[k].output_grad);
+    p.gdata = static_cast<S*>(g[k].data_grad);
+    p.gfwd = reinterpret_cast<S*>(wf);
+    wf += size_t(n) * C * sizeof(S);
+    p.glut = reinterpret_cast<S*>(wl);
+    wl += size_t(n) * 3 * sizeof(S);
+    p.gface[0] = static_cast<S*>(g[k].vel_x_grad);
+    p.gface[1] = static_cast<S*>(g[k].vel_y_grad);
+    p.gface[2] = static_cast<S*>(g[k].vel_z_grad);
+    p.dt = g[k].fwd.dt;
+    bb.item[k] = p;
+    bb.lk[k] = centered<T>(&g[k].fwd);
+    z += int(g[k].fwd.grid_dhw[0]);
+    bb.z_end[k] = z;
+  }
+  if (cudaMemsetAsync(ws, 0, gfwd_bytes, st) != cudaSuccess) return check_launch("advect batch memset");
+  const dim3 grid = batch_grid(maxw, maxh, zsum), block(32, 8);
+  k_mc_batch<C, T, CenteredLookup<T>, 2><<<grid, block, 0, st>>>(bb);
+  k_mc_batch<C, T, CenteredLookup<T>, 3><<<grid, block, 0, st>>>(bb);
+  return check_launch("ngt_advect_maccormack_bwd_batch");
+}
+
+template <class T>
+int batch_fwd_c(const ngt_advect_args* const* a, int count, int zsum, int mw, int mh, cudaStream_t st) {
+  switch (a[0]->channels) {
+    case 1: return density_fwd_batch<1, T>(a, count, zsum, mw, mh, st);
+    case 2: return density_fwd_batch<2, T>(a, count, zsum, mw, mh, st);
+    default: return density_fwd_batch<4, T>(a, count, zsum, mw, mh, st);
+  }
+}
+
+template <class T>
+int batch_bwd_c(const ngt_advect_grad_args* g, int count, int zsum, int mw, int mh, void* ws, cudaStream_t st) {
+  switch (g[0].fwd.channels) {
+    case 1: return density_bwd_batch<1, T>(g, count, zsum, mw, mh, ws, st);
+    case 2: return density_bwd_batch<2, T>(g, count, zsum, mw, mh, ws, st);
+    default: return density_bwd_batch<4, T>(g, count, zsum, mw, mh, ws, st);
+  }
+}
+
 }  // namespace
 }  // namespace ngt
 
@@ -811,5 +994,54 @@ extern "C" int ngt_advect_velocity_bwd(const ngt_advect_velocity_grad_args* g, v
     case NGT_F64: return vel_bwd<double>(g, st);
     case NGT_BF16: return vel_bwd<__nv_bfloat16>(g, st);
     default: return vel_bwd<__half>(g, st);
+  }
+}
+
+extern "C" int ngt_advect_maccormack_fwd_batch(const ngt_advect_args* items, int32_t count, void* stream) {
+  if (!items) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: null grids");
+  const ngt_advect_args* a[kMaxAdvBatch];
+  if (count < 1 || count > kMaxAdvBatch) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: 1 to %d grids", kMaxAdvBatch);
+  for (int i = 0; i < count; ++i) a[i] = items + i;
+  int zsum, mw, mh;
+  const int rc = validate_batch(a, count, zsum, mw, mh);
+  if (rc) return rc;
+  cudaStream_t st = as_stream(stream);
+  switch (items[0].dtype) {
+    case NGT_F32: return batch_fwd_c<float>(a, count, zsum, mw, mh, st);
+    case NGT_F64: return batch_fwd_c<double>(a, count, zsum, mw, mh, st);
+    case NGT_BF16: return batch_fwd_c<__nv_bfloat16>(a, count, zsum, mw, mh, st);
+    default: return batch_fwd_c<__half>(a, count, zsum, mw, mh, st);
+  }
+}
+
+extern "C" size_t ngt_advect_maccormack_bwd_batch_workspace_bytes(const ngt_advect_grad_args* items, int32_t count) {
+  return (items && count > 0 && count <= kMaxAdvBatch) ? batch_bwd_bytes(items, count) : 0;
+}
+
+extern "C" int ngt_advect_maccormack_bwd_batch(const ngt_advect_grad_args* items, int32_t count, void* workspace,
+                                               size_t workspace_bytes, void* stream) {
+  if (!items) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: null grids");
+  if (count < 1 || count > kMaxAdvBatch) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: 1 to %d grids", kMaxAdvBatch);
+  const ngt_advect_args* a[kMaxAdvBatch];
+  for (int i = 0; i < count; ++i) {
+    const ngt_advect_grad_args& g = items[i];
+    a[i] = &g.fwd;
+    if (!g.output_grad || !g.data_grad || !g.vel_x_grad || !g.vel_y_grad || !g.vel_z_grad)
+      return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch backward: null pointer");
+    if (g.grad_mode != NGT_GRAD_EXACT || g.deterministic)
+      return fail(NGT_ERR_UNSUPPORTED, "advect batch backward: exact, non-deterministic gradients only");
+  }
+  int zsum, mw, mh;
+  const int rc = validate_batch(a, count, zsum, mw, mh);
+  if (rc) return rc;
+  const size_t need = batch_bwd_bytes(items, count);
+  if (!workspace || workspace_bytes < need)
+    return fail(NGT_ERR_WORKSPACE, "advect batch backward needs %zu workspace bytes", need);
+  cudaStream_t st = as_stream(stream);
+  switch (items[0].fwd.dtype) {
+    case NGT_F32: return batch_bwd_c<float>(items, count, zsum, mw, mh, workspace, st);
+    case NGT_F64: return batch_bwd_c<double>(items, count, zsum, mw, mh, workspace, st);
+    case NGT_BF16: return batch_bwd_c<__nv_bfloat16>(items, count, zsum, mw, mh, workspace, st);
+    default: return batch_bwd_c<__half>(items, count, zsum, mw, mh, workspace, st);
   }
 }

@@ -79,6 +79,8 @@ __device__ __forceinline__ void slot_to_bc(const RayParams& p, int slot, int& b,
   oslot = slot;
 }
 
+__host__ __device__ __forceinline__ int num_slots_dev(const RayParams& p) { return p.sep ? p.N * p.ncam : p.N; }
+
 __device__ __forceinline__ void pixel_of_thread(int& px, int& py) {
   const int t = threadIdx.x;
   const int lane = t & 31, warp = t >> 5;
@@ -234,20 +236,20 @@ __global__ void k_build_cams(RayParams p, Cam* __restrict__ cams) {
 }
 
 // ----------------------------------------------------------------- forward
-template <int CIN, int CB, class T, class S>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_fwd(RayParams p) {
-  __shared__ Cam cam;
-  __shared__ CamScratch cam_sh;
-  int b, c, oslot;
-  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
-  __syncthreads();
+// This thread's pixel of tile ``tile`` of a W x H image; false outside the image.
+__device__ __forceinline__ bool tile_pixel(const RayParams& p, int tile, int& px, int& py) {
   const int tiles_x = (p.W + kTileX - 1) / kTileX;
-  int px, py;
   pixel_of_thread(px, py);
-  px += (blockIdx.x % tiles_x) * kTileX;
-  py += (blockIdx.x / tiles_x) * kTileY;
-  if (px >= p.W || py >= p.H) return;
+  px += (tile % tiles_x) * kTileX;
+  py += (tile / tiles_x) * kTileY;
+  return px < p.W && py < p.H;
+}
+
+// The forward of one 16x8 tile of rays of (batch b, output slot oslot).
+template <int CIN, int CB, class T, class S>
+__device__ __forceinline__ void fwd_tile(const RayParams& p, const Cam& cam, int b, int oslot, int tile) {
+  int px, py;
+  if (!tile_pixel(p, tile, px, py)) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
   const void* qg = quad_of<CIN, T>(p, b);
   const Ray r = ray_setup(cam, px, py, p);
@@ -269,25 +271,25 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_fwd(RayParams
   for (int k = 0; k < CB; ++k) out[k] = acc[k];
 }
 
-// ------------------------------------------------------- exact backward
-// Accumulator states are recomputed forward (checkpoints every K steps, then
-// each segment re-marched into a small buffer and walked back), so the adjoint
-// uses the forward's own positions and densities, not a subtraction.
 template <int CIN, int CB, class T, class S>
-__global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
-  if (p.flag && *p.flag == 0) return;  // Beer-Lambert with non-negative extinction: k_raymarch_bwd_bl
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_fwd(RayParams p) {
   __shared__ Cam cam;
   __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
   load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
   __syncthreads();
-  const int tiles_x = (p.W + kTileX - 1) / kTileX;
+  fwd_tile<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
+}
+
+// ------------------------------------------------------- exact backward
+// Accumulator states are recomputed forward (checkpoints every K steps, then
+// each segment re-marched into a small buffer and walked back), so the adjoint
+// uses the forward's own positions and densities, not a subtraction.
+template <int CIN, int CB, class T, class S>
+__device__ __forceinline__ void bwd_exact_tile(const RayParams& p, const Cam& cam, int b, int oslot, int tile) {
   int px, py;
-  pixel_of_thread(px, py);
-  px += (blockIdx.x % tiles_x) * kTileX;
-  py += (blockIdx.x / tiles_x) * kTileY;
-  if (px >= p.W || py >= p.H) return;
+  if (!tile_pixel(p, tile, px, py)) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
   const void* qg = quad_of<CIN, T>(p, b);
   S* grad = reinterpret_cast<S*>(p.in_grad) + int64_t(b) * p.din.count() * CIN;
@@ -374,6 +376,18 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
   }
 }
 
+template <int CIN, int CB, class T, class S>
+__global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
+  if (p.flag && *p.flag == 0) return;  // Beer-Lambert with non-negative extinction: k_raymarch_bwd_bl
+  __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
+  int b, c, oslot;
+  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
+  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
+  __syncthreads();
+  bwd_exact_tile<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
+}
+
 // ------------------------------------ exact Beer-Lambert backward, one pass
 // With every extinction sample sigma_k >= 0 the density never reaches the
 // max(d + sigma, 0) clamp, and the adjoint of the front-to-back blend
@@ -386,20 +400,9 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
 // extinction channel is checked over the whole grid first (k_extinction_sign),
 // and a launch that can see a negative sample runs k_raymarch_bwd_exact.
 template <int CIN, int CB, class T, class S>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(RayParams p) {
-  if (*p.flag != 0) return;
-  __shared__ Cam cam;
-  __shared__ CamScratch cam_sh;
-  int b, c, oslot;
-  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
-  __syncthreads();
-  const int tiles_x = (p.W + kTileX - 1) / kTileX;
+__device__ __forceinline__ void bwd_bl_tile(const RayParams& p, const Cam& cam, int b, int oslot, int tile) {
   int px, py;
-  pixel_of_thread(px, py);
-  px += (blockIdx.x % tiles_x) * kTileX;
-  py += (blockIdx.x / tiles_x) * kTileY;
-  if (px >= p.W || py >= p.H) return;
+  if (!tile_pixel(p, tile, px, py)) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
   const void* qg = quad_of<CIN, T>(p, b);
   S* grad = reinterpret_cast<S*>(p.in_grad) + int64_t(b) * p.din.count() * CIN;
@@ -433,6 +436,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(RayPar
 #pragma unroll
     for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
   }
+}
+
+template <int CIN, int CB, class T, class S>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(RayParams p) {
+  if (*p.flag != 0) return;
+  __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
+  int b, c, oslot;
+  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
+  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
+  __syncthreads();
+  bwd_bl_tile<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
 }
 
 // Sets *flag when some voxel makes a negative extinction sample possible: a
@@ -654,6 +669,117 @@ int launch_dtype(int dtype, int which, int cin, int cb, dim3 grid, cudaStream_t 
     case NGT_F16: return launch_typed<__half, float>(which, cin, cb, grid, st, p);
   }
   return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: invalid dtype");
+}
+
+// ------------------------------------------------------ batched, persistent
+// Many scenes of different grid, image and depth sizes in one launch: every
+// (scene, camera, 16x8 tile) is one work item, taken by persistent blocks from
+// a global counter; each block copies its item's camera from the per-scene
+// camera block and runs the same tile code as the single-scene kernels.
+constexpr int kMaxBatch = 32;
+
+struct RayBatch {
+  RayParams item[kMaxBatch];
+  int tile_end[kMaxBatch];        // cumulative work items over the scenes
+  int tiles_per_slot[kMaxBatch];  // tiles per (batch, camera) slot of each scene
+  int count, total;
+  int* counter;                   // work counter, zero at launch
+  int* flags;                     // backward: per-scene extinction-sign flags
+};
+
+template <int CIN, int CB, class T, class S, int WHICH>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_batch(const __grid_constant__ RayBatch bp) {
+  __shared__ Cam cam;
+  __shared__ int s_work;
+  for (;;) {
+    __syncthreads();  // the previous item's readers of cam and s_work are done
+    if (threadIdx.x == 0) s_work = atomicAdd(bp.counter, 1);
+    __syncthreads();
+    const int w = s_work;
+    if (w >= bp.total) return;
+    int it = 0;
+    while (it < bp.count - 1 && bp.tile_end[it] <= w) ++it;
+    const RayParams& p = bp.item[it];
+    const int local = w - (it ? bp.tile_end[it - 1] : 0);
+    const int slot = local / bp.tiles_per_slot[it], tile = local - slot * bp.tiles_per_slot[it];
+    // the one-pass backward takes scenes with non-negative extinction, the
+    // checkpointed one the others
+    const bool run = WHICH == FWD || (WHICH == BWD_BL ? (CB > 1 && bp.flags[it] == 0) : bp.flags[it] != 0);
+    if (!run) continue;
+    int b, c, oslot;
+    slot_to_bc(p, slot, b, c, oslot);
+    const float* src = reinterpret_cast<const float*>(p.cams + slot);
+    float* dst = reinterpret_cast<float*>(&cam);
+    for (int i = threadIdx.x; i < int(sizeof(Cam) / sizeof(float)); i += blockDim.x) dst[i] = __ldg(src + i);
+    __syncthreads();
+    if (WHICH == FWD)
+      fwd_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
+    else if (WHICH == BWD_BL)
+      bwd_bl_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
+    else
+      bwd_exact_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
+  }
+}
+
+// Cameras of every scene's slots (blockIdx.y = scene, blockIdx.x = slot).
+__global__ void k_build_cams_batch(const __grid_constant__ RayBatch bp) {
+  __shared__ Cam cam;
+  __shared__ CamScratch sh;
+  const RayParams& p = bp.item[blockIdx.y];
+  if (int(blockIdx.x) >= num_slots_dev(p)) return;
+  int b, c, oslot;
+  slot_to_bc(p, blockIdx.x, b, c, oslot);
+  build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, sh);
+  __syncwarp();
+  const float* src = reinterpret_cast<const float*>(&cam);
+  float* dst = reinterpret_cast<float*>(const_cast<Cam*>(p.cams) + blockIdx.x);
+  for (int i = threadIdx.x; i < int(sizeof(Cam) / sizeof(float)); i += 32) dst[i] = src[i];
+}
+
+// Extinction-sign check of every scene (blockIdx.y = scene) into bp.flags.
+template <int CIN, int CB, class T>
+__global__ void k_extinction_sign_batch(const __grid_constant__ RayBatch bp) {
+  const RayParams& p = bp.item[blockIdx.y];
+  const int64_t nvox = int64_t(p.N) * p.din.count();
+  const T* g = static_cast<const T*>(p.input);
+  int neg = 0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nvox; i += int64_t(gridDim.x) * blockDim.x) {
+    const float v = float(ld(g + i * CIN + (CIN - 1)));
+    neg |= (CIN == CB) ? (v < 0.0f) : (p.scale[CB - 1] * v < 0.0f);
+  }
+  if (__syncthreads_or(neg) && threadIdx.x == 0) atomicOr(bp.flags + blockIdx.y, 1);
+}
+
+template <int CIN, int CB, class T, class S>
+void launch_batch(int which, unsigned blocks, cudaStream_t st, const RayBatch& bp) {
+  if (which == FWD) {
+    k_raymarch_batch<CIN, CB, T, S, FWD><<<blocks, kThreads, 0, st>>>(bp);
+  } else if (which == BWD_BL) {
+    k_raymarch_batch<CIN, CB, T, S, BWD_BL><<<blocks, kThreads, 0, st>>>(bp);
+  } else if (which == BWD_EXACT) {
+    k_raymarch_batch<CIN, CB, T, S, BWD_EXACT><<<blocks, kThreads, 0, st>>>(bp);
+  } else {
+    k_extinction_sign_batch<CIN, CB, T><<<dim3(blocks, unsigned(bp.count)), 256, 0, st>>>(bp);
+  }
+}
+
+template <class T, class S>
+int launch_batch_typed(int which, int cin, int cb, unsigned blocks, cudaStream_t st, const RayBatch& bp) {
+  if (cin == 1 && cb == 2) launch_batch<1, 2, T, S>(which, blocks, st, bp);
+  else if (cin == 1 && cb == 4) launch_batch<1, 4, T, S>(which, blocks, st, bp);
+  else if (cin == 2 && cb == 2) launch_batch<2, 2, T, S>(which, blocks, st, bp);
+  else if (cin == 4 && cb == 4) launch_batch<4, 4, T, S>(which, blocks, st, bp);
+  else return fail(NGT_ERR_UNSUPPORTED, "raymarch batch: channels must be 1 (with emission 2 or 4), 2 or 4");
+  return NGT_OK;
+}
+
+int launch_batch_dtype(int dtype, int which, int cin, int cb, unsigned blocks, cudaStream_t st, const RayBatch& bp) {
+  switch (dtype) {
+    case NGT_F32: return launch_batch_typed<float, float>(which, cin, cb, blocks, st, bp);
+    case NGT_BF16: return launch_batch_typed<__nv_bfloat16, float>(which, cin, cb, blocks, st, bp);
+    case NGT_F16: return launch_batch_typed<__half, float>(which, cin, cb, blocks, st, bp);
+  }
+  return fail(NGT_ERR_UNSUPPORTED, "raymarch batch: float or 16-bit storage");
 }
 
 size_t compute_size(int dtype) { return dtype == NGT_F64 ? 8 : 4; }
@@ -917,6 +1043,161 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
     }
   }
   return check_launch("ngt_raymarch_bwd");
+}
+
+// ------------------------------------------------------------ batched calls
+namespace ngt {
+namespace {
+
+int sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
+// Workspace of a batch: [work counters and per-scene flags, 256 bytes][cameras of each scene].
+size_t batch_bytes(const ngt_raymarch_args* items, int count) {
+  size_t n = 256;
+  for (int i = 0; i < count; ++i) n += cams_bytes(items + i);
+  return n;
+}
+
+// Validates the scenes and fills bp (scenes ordered by descending work); cameras
+// that the caller did not prepare are formed into the workspace.
+int make_batch(const ngt_raymarch_args* const* items, int count, char* ws, size_t ws_bytes, RayBatch& bp, int& cin,
+               int& cb, int order[kMaxBatch], cudaStream_t st) {
+  if (count < 1 || count > kMaxBatch) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: 1 to %d scenes", kMaxBatch);
+  int64_t work[kMaxBatch];
+  for (int i = 0; i < count; ++i) {
+    int ci, cbi;
+    const int rc = validate(items[i], ci, cbi);
+    if (rc) return rc;
+    if (i == 0) {
+      cin = ci;
+      cb = cbi;
+    } else if (ci != cin || cbi != cb || items[i]->dtype != items[0]->dtype) {
+      return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: scenes must share dtype and channels");
+    }
+    if (items[i]->dtype == NGT_F64) return fail(NGT_ERR_UNSUPPORTED, "raymarch batch: float or 16-bit storage");
+    order[i] = i;
+    work[i] = slots_of(items[i]) * items[i]->output_dhw[0] * items[i]->output_dhw[1] * items[i]->output_dhw[2];
+  }
+  for (int i = 1; i < count; ++i)  // descending work: large scenes first
+    for (int j = i; j > 0 && work[order[j]] > work[order[j - 1]]; --j) {
+      const int t = order[j];
+      order[j] = order[j - 1];
+      order[j - 1] = t;
+    }
+  if (!ws) return fail(NGT_ERR_WORKSPACE, "raymarch batch: null workspace");
+  size_t need = 256;
+  for (int i = 0; i < count; ++i) need += cams_bytes(items[i]);
+  if (ws_bytes < need) return fail(NGT_ERR_WORKSPACE, "raymarch batch: needs %zu workspace bytes", need);
+  bp = RayBatch{};
+  bp.count = count;
+  bp.counter = reinterpret_cast<int*>(ws);
+  bp.flags = reinterpret_cast<int*>(ws) + 2;
+  size_t off = 256;
+  int total = 0, max_slots = 0;
+  bool build = false;
+  for (int k = 0; k < count; ++k) {
+    const ngt_raymarch_args* a = items[order[k]];
+    RayParams p = make_params(a);
+    if (a->cameras) {
+      p.cams = static_cast<const Cam*>(a->cameras);
+    } else {
+      p.cams = reinterpret_cast<const Cam*>(ws + off);
+      build = true;
+    }
+    off += cams_bytes(a);
+    const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
+    const int slots = num_slots(p);
+    if (int64_t(total) + int64_t(tiles) * slots >= (int64_t(1) << 31))
+      return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: too many tiles");
+    total += tiles * slots;
+    max_slots = slots > max_slots ? slots : max_slots;
+    bp.item[k] = p;
+    bp.tiles_per_slot[k] = tiles;
+    bp.tile_end[k] = total;
+  }
+  bp.total = total;
+  if (build) {
+    if (max_slots > 65535 * 32) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: too many cameras");
+    k_build_cams_batch<<<dim3(unsigned(max_slots), unsigned(count)), 32, 0, st>>>(bp);
+  }
+  return NGT_OK;
+}
+
+unsigned persistent_blocks(int blocks_per_sm, int total) {
+  const int per = blocks_per_sm > 0 ? blocks_per_sm : kMinBlocks;
+  const int64_t n = int64_t(per) * sm_count();
+  return unsigned(n < total ? n : (total > 0 ? total : 1));
+}
+
+}  // namespace
+}  // namespace ngt
+
+extern "C" size_t ngt_raymarch_batch_workspace_bytes(const ngt_raymarch_args* items, int32_t count) {
+  return (items && count > 0) ? batch_bytes(items, count) : 0;
+}
+
+extern "C" int ngt_raymarch_fwd_batch(const ngt_raymarch_args* items, int32_t count, int32_t blocks_per_sm,
+                                      void* workspace, size_t workspace_bytes, void* stream) {
+  if (!items) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null scenes");
+  const ngt_raymarch_args* ptrs[kMaxBatch];
+  if (count < 1 || count > kMaxBatch) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: 1 to %d scenes", kMaxBatch);
+  for (int i = 0; i < count; ++i) {
+    ptrs[i] = items + i;
+    if (!items[i].output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null output");
+  }
+  cudaStream_t st = as_stream(stream);
+  RayBatch bp;
+  int cin = 0, cb = 0, order[kMaxBatch];
+  int rc = make_batch(ptrs, count, static_cast<char*>(workspace), workspace_bytes, bp, cin, cb, order, st);
+  if (rc) return rc;
+  if (cudaMemsetAsync(workspace, 0, 256, st) != cudaSuccess) return check_launch("raymarch batch memset");
+  rc = launch_batch_dtype(items[0].dtype, FWD, cin, cb, persistent_blocks(blocks_per_sm, bp.total), st, bp);
+  if (rc) return rc;
+  return check_launch("ngt_raymarch_fwd_batch");
+}
+
+extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32_t blocks_per_sm,
+                                      void* workspace, size_t workspace_bytes, void* stream) {
+  if (!items) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null scenes");
+  if (count < 1 || count > kMaxBatch) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: 1 to %d scenes", kMaxBatch);
+  const ngt_raymarch_args* ptrs[kMaxBatch];
+  for (int i = 0; i < count; ++i) {
+    const ngt_raymarch_grad_args& g = items[i];
+    if (!g.output || !g.output_grad || !g.input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null pointer");
+    if (g.grad_mode != NGT_GRAD_EXACT || g.fwd.blending_mode != NGT_BEER_LAMBERT || g.fwd.interpolation != NGT_LINEAR)
+      return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: exact Beer-Lambert gradients of LINEAR sampling");
+    ptrs[i] = &g.fwd;
+  }
+  cudaStream_t st = as_stream(stream);
+  RayBatch bp;
+  int cin = 0, cb = 0, order[kMaxBatch];
+  int rc = make_batch(ptrs, count, static_cast<char*>(workspace), workspace_bytes, bp, cin, cb, order, st);
+  if (rc) return rc;
+  if (cb < 2) return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: Beer-Lambert needs 2 or 4 blend channels");
+  for (int k = 0; k < count; ++k) {
+    RayParams& p = bp.item[k];
+    p.out_fwd = items[order[k]].output;
+    p.out_grad = items[order[k]].output_grad;
+    p.in_grad = items[order[k]].input_grad;
+    if (cudaMemsetAsync(p.in_grad, 0, size_t(p.N) * p.din.count() * cin * sizeof(float), st) != cudaSuccess)
+      return check_launch("raymarch batch memset");
+  }
+  if (cudaMemsetAsync(workspace, 0, 256, st) != cudaSuccess) return check_launch("raymarch batch memset");
+  const int dtype = items[0].fwd.dtype;
+  rc = launch_batch_dtype(dtype, SIGN, cin, cb, unsigned(sm_count() * 2), st, bp);
+  if (rc) return rc;
+  const unsigned blocks = persistent_blocks(blocks_per_sm, bp.total);
+  rc = launch_batch_dtype(dtype, BWD_BL, cin, cb, blocks, st, bp);
+  if (rc) return rc;
+  bp.counter += 1;  // second persistent pass (scenes with possibly negative extinction)
+  rc = launch_batch_dtype(dtype, BWD_EXACT, cin, cb, blocks, st, bp);
+  if (rc) return rc;
+  return check_launch("ngt_raymarch_bwd_batch");
 }
 
 // ------------------------------------------ backward without caller memory

@@ -78,6 +78,36 @@ def config3():
     return plume_chain()
 
 
+def batched_scenes(n=32, seed=4, sizes=tuple(range(48, 161, 8)), cameras=(1, 8), image_sides=tuple(range(64, 257, 16)),
+                   depths=tuple(range(32, 129, 8)), max_u=1.0):
+    """Scenes of uneven size: each axis size drawn from ``sizes`` independently,
+    1-8 cameras on random yaws, square images with the side from ``image_sides``
+    and the depth from ``depths``.  Density blobs, curl-noise velocity and a
+    perturbed target density per scene (targets rendered by the caller)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        D, H, W = (int(v) for v in rng.choice(sizes, 3))
+        nv = int(rng.integers(cameras[0], cameras[1] + 1))
+        side = int(rng.choice(image_sides))
+        depth = int(rng.choice(depths))
+        yaws = list(rng.uniform(-90.0, 90.0, nv))
+        rho = synthetic.gaussian_blobs((D, H, W), n=4, seed=1000 + k)
+        rho_t = synthetic.gaussian_blobs((D, H, W), n=4, seed=1000 + k, amp_noise=0.05, noise_seed=2000 + k)
+        ux, uy, uz = synthetic.curl_noise_mac((D, H, W), max_u=max_u, seed=3000 + k)
+        cams = scene.orbit_cameras([depth, side, side], yaws)
+        V, P, F = scene.camera_params(cams)
+        M = scene.model_params([scene.volume_transform([D, H, W])])
+        out.append(Workload(rho=rho, rho_target=rho_t, ux=ux, uy=uy, uz=uz, M=M, V=V, P=P, F=F,
+                            image_dhw=(depth, side, side), grid=(D, H, W), views=nv, depth_step=cams[0].depth_step))
+    return out
+
+
+def config4():
+    """32 scenes, axis sizes 48-160, 1-8 cameras, images 64-256, depth 32-128."""
+    return batched_scenes()
+
+
 def algorithmic_bytes(grid, views, image, elem=4):
     """Compulsory HBM bytes of one differentiated step: every tensor that must
     cross HBM counted once at its storage size (density read / advected write /
