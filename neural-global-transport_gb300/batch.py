@@ -177,37 +177,51 @@ class BatchedScenes:
         return tuple(self.grads[k])
 
     # ------------------------------------------------------------ comparison
-    def per_scene(self):
-        """The same step with one single-scene library call per scene and operator."""
+    def _per_scene_args(self):
+        """Single-scene argument structs with their own workspaces (built once)."""
+        if getattr(self, "_single", None) is not None:
+            return self._single
+        dev = self.images.device
+        ray, ray_g, adv_g = [], [], []
+        for k in range(self.n):
+            r = L.RaymarchArgs.from_buffer_copy(self.ray[k])
+            ws = self.keep_ws(int(self.lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))), dev)
+            r.workspace, r.workspace_bytes = _ptr(ws), ws.numel()
+            ray.append(r)
+            g = L.RaymarchGradArgs.from_buffer_copy(self.ray_g[k])
+            ws = self.keep_ws(int(self.lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g))), dev)
+            g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
+            ray_g.append(g)
+            a = L.AdvectGradArgs.from_buffer_copy(self.adv_g[k])
+            ws = self.keep_ws(int(self.lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(a))), dev)
+            a.workspace, a.workspace_bytes = _ptr(ws), ws.numel()
+            adv_g.append(a)
+        self._single = (ray, ray_g, adv_g)
+        return self._single
+
+    def keep_ws(self, nbytes, dev):
+        t = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
+        self.keep.append(t)
+        return t
+
+    def per_scene_launch(self):
+        """Enqueue the same step with one single-scene library call per scene and operator."""
+        ray, ray_g, adv_g = self._per_scene_args()
         s = self._stream()
         self.loss.zero_()
-        dev = self.images.device
-        fws = []
         for k in range(self.n):
             self._call("ngt_advect_maccormack_fwd", ctypes.byref(self.adv[k]), s)
         for k in range(self.n):
-            r = L.RaymarchArgs.from_buffer_copy(self.ray[k])
-            ws = torch.empty(int(self.lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))), dtype=torch.uint8,
-                             device=dev)
-            fws.append(ws)
-            r.workspace, r.workspace_bytes = _ptr(ws), ws.numel()
-            self._call("ngt_raymarch_fwd", ctypes.byref(r), s)
+            self._call("ngt_raymarch_fwd", ctypes.byref(ray[k]), s)
         self._call("ngt_image_l2_loss", _code(self.images), self.pixels, 2, 1, _ptr(self.images),
                    _ptr(self.targets), _ptr(self.g_images), _ptr(self.loss), s)
         for k in range(self.n):
-            g = L.RaymarchGradArgs.from_buffer_copy(self.ray_g[k])
-            ws = torch.empty(int(self.lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g))), dtype=torch.uint8,
-                             device=dev)
-            fws.append(ws)
-            g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
-            self._call("ngt_raymarch_bwd", ctypes.byref(g), s)
+            self._call("ngt_raymarch_bwd", ctypes.byref(ray_g[k]), s)
         for k in range(self.n):
-            g = L.AdvectGradArgs.from_buffer_copy(self.adv_g[k])
-            ws = torch.empty(int(self.lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g))),
-                             dtype=torch.uint8, device=dev)
-            fws.append(ws)
-            g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
-            self._call("ngt_advect_maccormack_bwd", ctypes.byref(g), s)
+            self._call("ngt_advect_maccormack_bwd", ctypes.byref(adv_g[k]), s)
+
+    def per_scene(self):
+        self.per_scene_launch()
         torch.cuda.current_stream().synchronize()
         return self.loss
 

@@ -509,18 +509,25 @@ template <class T, class LK>
 struct McBatch {
   McParams<T> item[kMaxAdvBatch];
   LK lk[kMaxAdvBatch];
-  int z_end[kMaxAdvBatch];  // cumulative z planes
+  int block_end[kMaxAdvBatch];  // cumulative 32x8-cell blocks over the grids
+  int nbx[kMaxAdvBatch];        // blocks per row of each grid
+  int nby[kMaxAdvBatch];        // block rows per plane of each grid
   int count;
 };
 
+// One 32x8 block of cells of one grid per CUDA block, the grids' blocks back to
+// back in a 1-D launch (no idle blocks for the smaller grids).
 template <int C, class T, class LK, int PHASE>
 __global__ void __launch_bounds__(kBlock) k_mc_batch(const __grid_constant__ McBatch<T, LK> bb) {
   int it = 0;
-  const int zz = int(blockIdx.z);
-  while (it < bb.count - 1 && bb.z_end[it] <= zz) ++it;
+  const int w = int(blockIdx.x);
+  while (it < bb.count - 1 && bb.block_end[it] <= w) ++it;
   const McParams<T>& p = bb.item[it];
-  const int z = zz - (it ? bb.z_end[it - 1] : 0);
-  int x = int(blockIdx.x * blockDim.x + threadIdx.x), y = int(blockIdx.y * blockDim.y + threadIdx.y);
+  const int local = w - (it ? bb.block_end[it - 1] : 0);
+  const int per_plane = bb.nbx[it] * bb.nby[it];
+  const int z = local / per_plane, r = local - z * per_plane;
+  const int by = r / bb.nbx[it], bx = r - by * bb.nbx[it];
+  int x = bx * 32 + int(threadIdx.x), y = by * 8 + int(threadIdx.y);
   const bool active = x < p.d.x && y < p.d.y;
   if (PHASE == 0) {
     if (active) mc_fwd1_at<C>(p, bb.lk[it], x, y, z);
@@ -803,38 +810,44 @@ int validate_batch(const ngt_advect_args* const* a, int count, int& zsum, int& m
   if (count < 1 || count > kMaxAdvBatch)
     return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: 1 to %d grids", kMaxAdvBatch);
   zsum = maxw = maxh = 0;
+  int64_t blocks = 0;
   for (int i = 0; i < count; ++i) {
     const int rc = validate(a[i]);
     if (rc) return rc;
     if (!a[i]->output) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null output");
     if (a[i]->dtype != a[0]->dtype || a[i]->channels != a[0]->channels)
       return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: grids must share dtype and channels");
-    zsum += int(a[i]->grid_dhw[0]);
-    maxw = max(maxw, int(a[i]->grid_dhw[2]));
-    maxh = max(maxh, int(a[i]->grid_dhw[1]));
+    blocks += ((a[i]->grid_dhw[2] + 31) / 32) * ((a[i]->grid_dhw[1] + 7) / 8) * a[i]->grid_dhw[0];
   }
-  if (zsum > 65535) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: more than 65535 z planes in total");
+  if (blocks >= (int64_t(1) << 31)) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: grids too large");
   return NGT_OK;
 }
 
-dim3 batch_grid(int maxw, int maxh, int zsum) {
-  return dim3(unsigned((maxw + 31) / 32), unsigned((maxh + 7) / 8), unsigned(zsum));
+// Fills the 1-D block table of a batch; returns the number of blocks.
+template <class T, class LK>
+int block_table(McBatch<T, LK>& bb) {
+  int total = 0;
+  for (int k = 0; k < bb.count; ++k) {
+    const Dims& d = bb.item[k].d;
+    bb.nbx[k] = (d.x + 31) / 32;
+    bb.nby[k] = (d.y + 7) / 8;
+    total += bb.nbx[k] * bb.nby[k] * d.z;
+    bb.block_end[k] = total;
+  }
+  return total;
 }
 
 template <int C, class T>
 int density_fwd_batch(const ngt_advect_args* const* a, int count, int zsum, int maxw, int maxh, cudaStream_t st) {
   McBatch<T, CenteredLookup<T>> bb{};
   bb.count = count;
-  int z = 0;
   bool mc = false;
   for (int k = 0; k < count; ++k) {
     bb.item[k] = density_params<T>(a[k]);
     bb.lk[k] = centered<T>(a[k]);
-    z += int(a[k]->grid_dhw[0]);
-    bb.z_end[k] = z;
     mc = mc || a[k]->order == 2;
   }
-  const dim3 grid = batch_grid(maxw, maxh, zsum), block(32, 8);
+  const dim3 grid(unsigned(block_table(bb))), block(32, 8);
   k_mc_batch<C, T, CenteredLookup<T>, 0><<<grid, block, 0, st>>>(bb);
   if (mc) k_mc_batch<C, T, CenteredLookup<T>, 1><<<grid, block, 0, st>>>(bb);
   return check_launch("ngt_advect_maccormack_fwd_batch");
@@ -863,7 +876,6 @@ int density_bwd_batch(const ngt_advect_grad_args* g, int count, int zsum, int ma
     gfwd_bytes += size_t(g[k].fwd.grid_dhw[0] * g[k].fwd.grid_dhw[1] * g[k].fwd.grid_dhw[2]) * C * sizeof(S);
   char* wf = static_cast<char*>(ws);
   char* wl = wf + gfwd_bytes;
-  int z = 0;
   for (int k = 0; k < count; ++k) {
     McParams<T> p = density_params<T>(&g[k].fwd);
     const int64_t n = p.d.count();
@@ -879,11 +891,9 @@ int density_bwd_batch(const ngt_advect_grad_args* g, int count, int zsum, int ma
     p.dt = g[k].fwd.dt;
     bb.item[k] = p;
     bb.lk[k] = centered<T>(&g[k].fwd);
-    z += int(g[k].fwd.grid_dhw[0]);
-    bb.z_end[k] = z;
   }
   if (cudaMemsetAsync(ws, 0, gfwd_bytes, st) != cudaSuccess) return check_launch("advect batch memset");
-  const dim3 grid = batch_grid(maxw, maxh, zsum), block(32, 8);
+  const dim3 grid(unsigned(block_table(bb))), block(32, 8);
   k_mc_batch<C, T, CenteredLookup<T>, 2><<<grid, block, 0, st>>>(bb);
   k_mc_batch<C, T, CenteredLookup<T>, 3><<<grid, block, 0, st>>>(bb);
   return check_launch("ngt_advect_maccormack_bwd_batch");

@@ -65,12 +65,10 @@ __device__ __forceinline__ uint32_t raw16(T v) {
 // With ``neg`` set it also raises *neg when scale * value < 0 for some cell (the
 // extinction-sign check of the raymarch backward).
 template <class T>
-__global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename QuadOf<T>::type* __restrict__ q,
-                             int* neg, float scale) {
+__device__ __forceinline__ void quad_build_at(const T* __restrict__ g, const Dims& d, int bm,
+                                              typename QuadOf<T>::type* __restrict__ q, int* neg, float scale, int xq,
+                                              int yq, int zq, int b) {
   const QuadDims qd = QuadDims::of(d);
-  const int xq = int(blockIdx.x * blockDim.x + threadIdx.x), yq = int(blockIdx.y * blockDim.y + threadIdx.y);
-  if (xq >= qd.x || yq >= qd.y) return;
-  const int b = int(blockIdx.z) / qd.z, zq = int(blockIdx.z) - b * qd.z;
   const int64_t e = (int64_t(zq) * qd.y + yq) * qd.x + xq;
   bool vz;
   const int z = quad_cell(zq - 1, d.z, bm, vz);
@@ -97,6 +95,16 @@ __global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename Q
     o.y = raw16(v[2]) | (raw16(v[3]) << 16);
   }
   q[int64_t(b) * qd.count + e] = o;
+}
+
+template <class T>
+__global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename QuadOf<T>::type* __restrict__ q,
+                             int* neg, float scale) {
+  const QuadDims qd = QuadDims::of(d);
+  const int xq = int(blockIdx.x * blockDim.x + threadIdx.x), yq = int(blockIdx.y * blockDim.y + threadIdx.y);
+  if (xq >= qd.x || yq >= qd.y) return;
+  const int b = int(blockIdx.z) / qd.z, zq = int(blockIdx.z) - b * qd.z;
+  quad_build_at<T>(g, d, bm, q, neg, scale, xq, yq, zq, b);
 }
 
 template <class T>
@@ -212,11 +220,9 @@ __device__ __forceinline__ int quad_sources(int i, int n, int bm, int src[3]) {
 // thread per cell, launched as cell_launch over W, H and D * N planes
 // (blockIdx.z = z + D * b).  Component (kx, ky) of entry (xq, yq) is coordinate
 // (xq - 1 + kx, yq - 1 + ky) of plane zq - 1.
-__global__ void k_quad_fold(const float4* __restrict__ gq, Dims d, int bm, float* __restrict__ grad) {
+__device__ __forceinline__ void quad_fold_at(const float4* __restrict__ gq, const Dims& d, int bm,
+                                             float* __restrict__ grad, int x, int y, int z, int b) {
   const QuadDims qd = QuadDims::of(d);
-  const int x = int(blockIdx.x * blockDim.x + threadIdx.x), y = int(blockIdx.y * blockDim.y + threadIdx.y);
-  if (x >= d.x || y >= d.y) return;
-  const int b = int(blockIdx.z) / d.z, z = int(blockIdx.z) - b * d.z;
   const int64_t i = (int64_t(z) * d.y + y) * d.x + x;
   const float4* q = gq + int64_t(b) * qd.count;
   int sx[3], sy[3], sz[3];
@@ -238,6 +244,13 @@ __global__ void k_quad_fold(const float4* __restrict__ gq, Dims d, int bm, float
     }
   }
   grad[int64_t(b) * d.count() + i] = acc;
+}
+
+__global__ void k_quad_fold(const float4* __restrict__ gq, Dims d, int bm, float* __restrict__ grad) {
+  const int x = int(blockIdx.x * blockDim.x + threadIdx.x), y = int(blockIdx.y * blockDim.y + threadIdx.y);
+  if (x >= d.x || y >= d.y) return;
+  const int b = int(blockIdx.z) / d.z, z = int(blockIdx.z) - b * d.z;
+  quad_fold_at(gq, d, bm, grad, x, y, z, b);
 }
 
 }  // namespace ngt

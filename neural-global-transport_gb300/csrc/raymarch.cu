@@ -17,6 +17,7 @@
 #include "ngt_blend.cuh"
 #include "ngt_quad.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace ngt {
@@ -685,10 +686,30 @@ struct RayBatch {
   int count, total;
   int* counter;                   // work counter, zero at launch
   int* flags;                     // backward: per-scene extinction-sign flags
+  // 32x8 blocks of the quad layouts and of the cell grids, back to back
+  int qblock_end[kMaxBatch], qnbx[kMaxBatch], qnby[kMaxBatch];
+  int cblock_end[kMaxBatch], cnbx[kMaxBatch], cnby[kMaxBatch];
 };
 
+// Scene, plane and in-plane position of this thread of a 1-D launch over the
+// scenes' 32x8 blocks (block_end / nbx / nby); false for padding threads.
+__device__ __forceinline__ bool batch_block(const int* block_end, const int* nbx, const int* nby, int count, int dx,
+                                            int dy, int& it, int& x, int& y, int& z) {
+  const int w = int(blockIdx.x);
+  it = 0;
+  while (it < count - 1 && block_end[it] <= w) ++it;
+  const int local = w - (it ? block_end[it - 1] : 0);
+  const int per_plane = nbx[it] * nby[it];
+  z = local / per_plane;
+  const int r = local - z * per_plane;
+  const int by = r / nbx[it], bx = r - by * nbx[it];
+  x = bx * 32 + int(threadIdx.x);
+  y = by * 8 + int(threadIdx.y);
+  return true;
+}
+
 template <int CIN, int CB, class T, class S, int WHICH>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_batch(const __grid_constant__ RayBatch bp) {
+__global__ void __launch_bounds__(kThreads, CIN == 1 ? 8 : 4) k_raymarch_batch(const __grid_constant__ RayBatch bp) {
   __shared__ Cam cam;
   __shared__ int s_work;
   for (;;) {
@@ -719,6 +740,30 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_batch(const _
     else
       bwd_exact_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
   }
+}
+
+// Quad layouts of every scene (blockIdx.z over the concatenated padded planes);
+// with flags, also each scene's extinction-sign check.
+template <class T>
+__global__ void k_quad_build_batch(const __grid_constant__ RayBatch bp, int with_flags, int cb) {
+  int it, xq, yq, zl;
+  batch_block(bp.qblock_end, bp.qnbx, bp.qnby, bp.count, 32, 8, it, xq, yq, zl);
+  const RayParams& p = bp.item[it];
+  if (xq >= p.qd.x || yq >= p.qd.y) return;
+  const int b = zl / p.qd.z, zq = zl - b * p.qd.z;
+  quad_build_at<T>(static_cast<const T*>(p.input), p.din, p.bm,
+                   static_cast<typename QuadOf<T>::type*>(const_cast<void*>(p.quad)),
+                   with_flags ? bp.flags + it : nullptr, cb > 1 ? p.scale[cb - 1] : 1.0f, xq, yq, zq, b);
+}
+
+// Cell gradients of every scene from its quad gradient (blockIdx.z over all planes).
+__global__ void k_quad_fold_batch(const __grid_constant__ RayBatch bp) {
+  int it, x, y, zl;
+  batch_block(bp.cblock_end, bp.cnbx, bp.cnby, bp.count, 32, 8, it, x, y, zl);
+  const RayParams& p = bp.item[it];
+  if (x >= p.din.x || y >= p.din.y) return;
+  const int b = zl / p.din.z, z = zl - b * p.din.z;
+  quad_fold_at(p.gquad, p.din, p.bm, static_cast<float*>(p.in_grad), x, y, z, b);
 }
 
 // Cameras of every scene's slots (blockIdx.y = scene, blockIdx.x = slot).
@@ -1056,10 +1101,22 @@ int sm_count() {
   return n > 0 ? n : 1;
 }
 
-// Workspace of a batch: [work counters and per-scene flags, 256 bytes][cameras of each scene].
-size_t batch_bytes(const ngt_raymarch_args* items, int count) {
+// Scenes that all take the quad layout (one channel, LINEAR, float / 16-bit).
+bool batch_quad(const ngt_raymarch_args* const* items, int count) {
+  for (int i = 0; i < count; ++i)
+    if (!quad_case(items[i])) return false;
+  return true;
+}
+
+// Workspace of a batch: [work counters and per-scene flags, 256 bytes][cameras of
+// each scene][quad layout of each scene][quad gradient of each scene].
+size_t batch_bytes(const ngt_raymarch_args* const* items, int count) {
   size_t n = 256;
-  for (int i = 0; i < count; ++i) n += cams_bytes(items + i);
+  const bool quad = batch_quad(items, count);
+  for (int i = 0; i < count; ++i) {
+    n += cams_bytes(items[i]);
+    if (quad) n += quad_bytes(items[i]) + gquad_bytes(items[i]);
+  }
   return n;
 }
 
@@ -1090,15 +1147,19 @@ int make_batch(const ngt_raymarch_args* const* items, int count, char* ws, size_
       order[j - 1] = t;
     }
   if (!ws) return fail(NGT_ERR_WORKSPACE, "raymarch batch: null workspace");
-  size_t need = 256;
-  for (int i = 0; i < count; ++i) need += cams_bytes(items[i]);
+  const size_t need = batch_bytes(items, count);
   if (ws_bytes < need) return fail(NGT_ERR_WORKSPACE, "raymarch batch: needs %zu workspace bytes", need);
   bp = RayBatch{};
   bp.count = count;
   bp.counter = reinterpret_cast<int*>(ws);
   bp.flags = reinterpret_cast<int*>(ws) + 2;
-  size_t off = 256;
-  int total = 0, max_slots = 0;
+  const bool quad = batch_quad(items, count);
+  size_t off = 256, qoff = 256, goff = 256;
+  for (int k = 0; k < count; ++k) qoff += cams_bytes(items[k]);
+  goff = qoff;
+  if (quad)
+    for (int k = 0; k < count; ++k) goff += quad_bytes(items[k]);
+  int total = 0, max_slots = 0, qz = 0, cz = 0;  // block counts of the quad and cell launches
   bool build = false;
   for (int k = 0; k < count; ++k) {
     const ngt_raymarch_args* a = items[order[k]];
@@ -1110,6 +1171,25 @@ int make_batch(const ngt_raymarch_args* const* items, int count, char* ws, size_
       build = true;
     }
     off += cams_bytes(a);
+    if (quad) {
+      p.quad = ws + qoff;
+      p.gquad = reinterpret_cast<float4*>(ws + goff);
+      p.qd = QuadDims::of(p.din);
+      qoff += quad_bytes(a);
+      goff += gquad_bytes(a);
+      bp.qnbx[k] = (p.qd.x + 31) / 32;
+      bp.qnby[k] = (p.qd.y + 7) / 8;
+      bp.cnbx[k] = (p.din.x + 31) / 32;
+      bp.cnby[k] = (p.din.y + 7) / 8;
+      const int64_t qb = int64_t(bp.qnbx[k]) * bp.qnby[k] * p.N * p.qd.z;
+      const int64_t cbk = int64_t(bp.cnbx[k]) * bp.cnby[k] * p.N * p.din.z;
+      if (int64_t(qz) + qb >= (int64_t(1) << 31) || int64_t(cz) + cbk >= (int64_t(1) << 31))
+        return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: grids too large");
+      qz += int(qb);
+      cz += int(cbk);
+      bp.qblock_end[k] = qz;
+      bp.cblock_end[k] = cz;
+    }
     const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
     const int slots = num_slots(p);
     if (int64_t(total) + int64_t(tiles) * slots >= (int64_t(1) << 31))
@@ -1137,8 +1217,29 @@ unsigned persistent_blocks(int blocks_per_sm, int total) {
 }  // namespace
 }  // namespace ngt
 
+namespace ngt {
+namespace {
+
+// Quad layouts of a batch (every scene's layout, and with flags the sign check).
+int build_quads_batch(int dtype, const RayBatch& bp, int with_flags, int cb, cudaStream_t st) {
+  const dim3 grid(unsigned(bp.qblock_end[bp.count - 1])), block(32, 8);
+  switch (dtype) {
+    case NGT_F32: k_quad_build_batch<float><<<grid, block, 0, st>>>(bp, with_flags, cb); break;
+    case NGT_BF16: k_quad_build_batch<__nv_bfloat16><<<grid, block, 0, st>>>(bp, with_flags, cb); break;
+    case NGT_F16: k_quad_build_batch<__half><<<grid, block, 0, st>>>(bp, with_flags, cb); break;
+    default: return fail(NGT_ERR_UNSUPPORTED, "raymarch batch: quad layout needs float or 16-bit storage");
+  }
+  return NGT_OK;
+}
+
+}  // namespace
+}  // namespace ngt
+
 extern "C" size_t ngt_raymarch_batch_workspace_bytes(const ngt_raymarch_args* items, int32_t count) {
-  return (items && count > 0) ? batch_bytes(items, count) : 0;
+  if (!items || count < 1 || count > kMaxBatch) return 0;
+  const ngt_raymarch_args* ptrs[kMaxBatch];
+  for (int i = 0; i < count; ++i) ptrs[i] = items + i;
+  return batch_bytes(ptrs, count);
 }
 
 extern "C" int ngt_raymarch_fwd_batch(const ngt_raymarch_args* items, int32_t count, int32_t blocks_per_sm,
@@ -1156,6 +1257,10 @@ extern "C" int ngt_raymarch_fwd_batch(const ngt_raymarch_args* items, int32_t co
   int rc = make_batch(ptrs, count, static_cast<char*>(workspace), workspace_bytes, bp, cin, cb, order, st);
   if (rc) return rc;
   if (cudaMemsetAsync(workspace, 0, 256, st) != cudaSuccess) return check_launch("raymarch batch memset");
+  if (bp.item[0].quad) {
+    rc = build_quads_batch(items[0].dtype, bp, 0, cb, st);
+    if (rc) return rc;
+  }
   rc = launch_batch_dtype(items[0].dtype, FWD, cin, cb, persistent_blocks(blocks_per_sm, bp.total), st, bp);
   if (rc) return rc;
   return check_launch("ngt_raymarch_fwd_batch");
@@ -1179,24 +1284,37 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
   int rc = make_batch(ptrs, count, static_cast<char*>(workspace), workspace_bytes, bp, cin, cb, order, st);
   if (rc) return rc;
   if (cb < 2) return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: Beer-Lambert needs 2 or 4 blend channels");
+  const bool quad = bp.item[0].quad != nullptr;
   for (int k = 0; k < count; ++k) {
     RayParams& p = bp.item[k];
     p.out_fwd = items[order[k]].output;
     p.out_grad = items[order[k]].output_grad;
     p.in_grad = items[order[k]].input_grad;
-    if (cudaMemsetAsync(p.in_grad, 0, size_t(p.N) * p.din.count() * cin * sizeof(float), st) != cudaSuccess)
+    // the quad path writes every cell gradient in its fold; the direct path adds
+    if (!quad && cudaMemsetAsync(p.in_grad, 0, size_t(p.N) * p.din.count() * cin * sizeof(float), st) != cudaSuccess)
       return check_launch("raymarch batch memset");
   }
   if (cudaMemsetAsync(workspace, 0, 256, st) != cudaSuccess) return check_launch("raymarch batch memset");
   const int dtype = items[0].fwd.dtype;
-  rc = launch_batch_dtype(dtype, SIGN, cin, cb, unsigned(sm_count() * 2), st, bp);
+  if (quad) {
+    // quad gradients are contiguous: from the first scene's to the end of the workspace layout
+    char* g0 = reinterpret_cast<char*>(bp.item[0].gquad);
+    for (int k = 1; k < count; ++k) g0 = std::min(g0, reinterpret_cast<char*>(bp.item[k].gquad));
+    const size_t gbytes = batch_bytes(ptrs, count) - size_t(g0 - static_cast<char*>(workspace));
+    if (cudaMemsetAsync(g0, 0, gbytes, st) != cudaSuccess) return check_launch("raymarch batch memset");
+    rc = build_quads_batch(dtype, bp, 1, cb, st);
+  } else {
+    rc = launch_batch_dtype(dtype, SIGN, cin, cb, unsigned(sm_count() * 2), st, bp);
+  }
   if (rc) return rc;
   const unsigned blocks = persistent_blocks(blocks_per_sm, bp.total);
   rc = launch_batch_dtype(dtype, BWD_BL, cin, cb, blocks, st, bp);
   if (rc) return rc;
-  bp.counter += 1;  // second persistent pass (scenes with possibly negative extinction)
-  rc = launch_batch_dtype(dtype, BWD_EXACT, cin, cb, blocks, st, bp);
+  RayBatch bp2 = bp;
+  bp2.counter += 1;  // second persistent pass: scenes with possibly negative extinction
+  rc = launch_batch_dtype(dtype, BWD_EXACT, cin, cb, blocks, st, bp2);
   if (rc) return rc;
+  if (quad) k_quad_fold_batch<<<unsigned(bp.cblock_end[count - 1]), dim3(32, 8), 0, st>>>(bp);
   return check_launch("ngt_raymarch_bwd_batch");
 }
 
