@@ -230,11 +230,15 @@ int ngt_raymarch_cameras(const ngt_raymarch_args* args, void* cameras, void* str
 int ngt_raymarch_fwd(const ngt_raymarch_args* args, void* stream);
 int ngt_raymarch_bwd(const ngt_raymarch_grad_args* args, void* stream);
 size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* args);
-/* ngt_raymarch_bwd for callers that cannot allocate device memory: no counterpart
- * in the reference.  args->workspace is ignored; the scratch is a 16 MiB static
- * device array shared by every call (calls needing more, see
- * ngt_raymarch_bwd_workspace_bytes, fail with NGT_ERR_WORKSPACE).  Calls whose
- * GPU work overlaps race on that array. */
+/* ngt_raymarch_bwd for callers that cannot allocate device memory -- a host
+ * program whose own pool owns the whole device, or a loop that may not allocate
+ * once it runs.  No counterpart in the reference.  args->workspace is ignored:
+ * the scratch is a 16 MiB static device array that every GPU using the library
+ * holds until exit, shared by all calls and keeping the last call's contents
+ * (each call clears what must start at zero).  Calls needing more (see
+ * ngt_raymarch_bwd_workspace_bytes) fail with NGT_ERR_WORKSPACE.  The first call
+ * on a device looks up the array's device address: make it before any stream
+ * capture.  Calls whose GPU work overlaps race on the array. */
 int ngt_raymarch_bwd_static(const ngt_raymarch_grad_args* args, void* stream);
 
 /* ------------------------------------------------------------ reduce blend */

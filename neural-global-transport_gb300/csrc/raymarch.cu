@@ -1319,19 +1319,26 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
 }
 
 // ------------------------------------------ backward without caller memory
-// For callers that cannot allocate device memory: the backward's scratch
-// (sign flag, cameras, quad layout and quad gradient) lives in one file-scope
-// device array of kStaticScratchBytes.  Every call shares it; what must start
-// at zero (the sign flag, the quad gradient, the reference-mode buffers) is
-// cleared inside each call by ngt_raymarch_bwd's own stream-ordered memsets.
-// Calls whose work overlaps on the GPU (other streams, other host threads)
-// race on the array.
+// Some callers cannot allocate device memory: a host program whose own pool
+// owns the whole device, or a loop that may not allocate once it is running.
+// ngt_raymarch_bwd_static serves them with the backward's scratch (sign flag,
+// cameras, quad layout and quad gradient) in one file-scope device array of
+// kStaticScratchBytes, which every GPU that loads the library holds until the
+// process exits.  Every call shares the array and finds the previous call's
+// contents in it; what must start at zero (the sign flag, the quad gradient,
+// the reference-mode buffers) is cleared inside each call by ngt_raymarch_bwd's
+// own stream-ordered memsets.  Calls whose work overlaps on the GPU (other
+// streams, other host threads) race on the array.  In host code the array's
+// name is only a stand-in: its device address is looked up with
+// cudaGetSymbolAddress by the first call on each device, with that device
+// current, and that first call should come before any stream capture.
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_raymarch_scratch[kStaticScratchBytes];
+
 namespace ngt {
 namespace {
 
-constexpr size_t kStaticScratchBytes = size_t(16) << 20;
 constexpr int kMaxDevices = 64;
-__device__ __align__(256) unsigned char g_raymarch_scratch[kStaticScratchBytes];
 
 std::mutex g_scratch_mutex;
 void* g_scratch_ptr[kMaxDevices] = {};

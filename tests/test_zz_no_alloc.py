@@ -1,5 +1,8 @@
-"""ngt_raymarch_bwd_static (scratch in a static device array, no caller memory)
-against ngt_raymarch_bwd with a caller workspace, through the C ABI.
+"""ngt_raymarch_bwd_static -- the render backward for callers that cannot
+allocate device memory (their host program's pool owns the device, or they may
+not allocate once running), with its scratch in a static device array --
+against ngt_raymarch_bwd with a caller workspace, through the C ABI, on two
+calls in a row (the second finds the first call's leftovers in the array).
 
 Collected last on purpose: it must pass both alone in a fresh process and after
 every other test has used the library."""
