@@ -284,6 +284,11 @@ typedef struct {
   int32_t boundary;           /* BORDER, CLAMP, WRAP (configs: CLAMP) */
   void* output;               /* D, H, W, C */
   void* fwd_field;            /* D, H, W, C scratch written by the forward (order 2), read by the backward */
+  /* Optional, MacCormack with MC_SMOOTH: one byte per cell and channel, the
+   * forward's revert mask (1 where the correction left the corners' range);
+   * the backward then reads it instead of re-gathering the corner extrema.
+   * Null: recomputed.  No reference counterpart (TF keeps the tf.where mask). */
+  void* mask;
 } ngt_advect_args;
 
 typedef struct {

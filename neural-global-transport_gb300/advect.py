@@ -32,7 +32,7 @@ def _faces(t, name):
     return t.contiguous()
 
 
-def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary):
+def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None):
     a = L.AdvectArgs()
     a.dtype = _code(data)
     D, H, W, C = data.shape
@@ -44,6 +44,7 @@ def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary):
     a.clamp = L.CLAMP[clamp.upper()]
     a.boundary = L.BOUNDARY[boundary]
     a.output, a.fwd_field = _ptr(out), _ptr(fwd)
+    a.mask = _ptr(mask)
     return a
 
 
@@ -54,20 +55,23 @@ def _check_faces(data, vx, vy, vz):
                          % (tuple(data.shape), tuple(vx.shape), tuple(vy.shape), tuple(vz.shape)))
 
 
-def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP"):
-    """Forward only; returns (output, fwd_field) with fwd_field kept for the backward."""
+def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP", keep_mask=False):
+    """Forward only; returns (output, fwd_field, mask) with fwd_field and the
+    MC_SMOOTH revert mask (when ``keep_mask``) kept for the backward."""
     out = torch.empty_like(data)
     fwd = torch.empty(data.shape, dtype=compute_dtype(data), device=data.device) if order == 2 else None
-    L.call("ngt_advect_maccormack_fwd", ctypes.byref(_args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary)),
-           _stream())
-    return out, fwd
+    mask = (torch.empty(data.shape, dtype=torch.uint8, device=data.device)
+            if keep_mask and order == 2 and clamp.upper() == "MC_SMOOTH" else None)
+    L.call("ngt_advect_maccormack_fwd",
+           ctypes.byref(_args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask)), _stream())
+    return out, fwd, mask
 
 
 def warp_backward(data, vx, vy, vz, fwd, grad, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP",
-                  grad_mode=None, velocity_grad=True, deterministic=None):
+                  grad_mode=None, velocity_grad=True, deterministic=None, mask=None):
     cd = compute_dtype(data)
     g = L.AdvectGradArgs()
-    g.fwd = _args(data, vx, vy, vz, None, fwd, dt, order, clamp, boundary)
+    g.fwd = _args(data, vx, vy, vz, None, fwd, dt, order, clamp, boundary, mask)
     gd = torch.empty(data.shape, dtype=cd, device=data.device)
     gx = torch.empty(vx.shape, dtype=cd, device=data.device) if velocity_grad else None
     gy = torch.empty(vy.shape, dtype=cd, device=data.device) if velocity_grad else None
@@ -86,17 +90,17 @@ def warp_backward(data, vx, vy, vz, fwd, grad, dt=1.0, order=2, clamp="MC_SMOOTH
 class _Warp(torch.autograd.Function):
     @staticmethod
     def forward(ctx, data, vx, vy, vz, dt, order, clamp, boundary):
-        out, fwd = warp_forward(data, vx, vy, vz, dt, order, clamp, boundary)
-        ctx.save_for_backward(data, vx, vy, vz, fwd)
+        out, fwd, mask = warp_forward(data, vx, vy, vz, dt, order, clamp, boundary, keep_mask=True)
+        ctx.save_for_backward(data, vx, vy, vz, fwd, mask)
         ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode(), get_deterministic())
         return out
 
     @staticmethod
     def backward(ctx, grad):
-        data, vx, vy, vz, fwd = ctx.saved_tensors
+        data, vx, vy, vz, fwd, mask = ctx.saved_tensors
         dt, order, clamp, boundary, mode, det = ctx.cfg
         gd, gx, gy, gz = warp_backward(data, vx, vy, vz, fwd, grad.contiguous(), dt, order, clamp, boundary, mode,
-                                       velocity_grad=any(ctx.needs_input_grad[1:4]), deterministic=det)
+                                       velocity_grad=any(ctx.needs_input_grad[1:4]), deterministic=det, mask=mask)
         return gd, gx, gy, gz, None, None, None, None
 
 

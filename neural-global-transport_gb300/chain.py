@@ -71,7 +71,10 @@ class AdvectRenderChain:
         self.g_u = [torch.empty(u.shape, dtype=cd, device=dev) for u in (ux, uy, uz)]
         self.g_u_frame = [torch.empty(u.shape, dtype=cd, device=dev) for u in (ux, uy, uz)]
 
-        def advect_args(data, out, fwd):
+        # MC_SMOOTH revert masks of the segment's frames (forward writes, backward reads)
+        self.seg_mask = torch.empty((K, D, H, W, 1), dtype=torch.uint8, device=dev)
+
+        def advect_args(data, out, fwd, mask=None):
             a = L.AdvectArgs()
             a.dtype = _code(rho0)
             a.grid_dhw = L.I64x3(D, H, W)
@@ -79,12 +82,14 @@ class AdvectRenderChain:
             a.data, a.vel_x, a.vel_y, a.vel_z = _ptr(data), _ptr(self.ux), _ptr(self.uy), _ptr(self.uz)
             a.dt, a.order, a.clamp, a.boundary = float(dt), 2, L.CLAMP[clamp], L.BOUNDARY[advect_boundary]
             a.output, a.fwd_field = _ptr(out), _ptr(fwd)
+            a.mask = _ptr(mask)
             return a
 
         # chain forward: cur[t % 2] -> cur[(t + 1) % 2]
         self.adv_chain = [advect_args(self.cur[k], self.cur[1 - k], self.chain_fwd) for k in range(2)]
         # segment recompute: seg[j] -> seg[j + 1], fwd field seg_fwd[j]
-        self.adv_seg = [advect_args(self.seg[j], self.seg[j + 1], self.seg_fwd[j]) for j in range(K)]
+        self.adv_seg = [advect_args(self.seg[j], self.seg[j + 1], self.seg_fwd[j], self.seg_mask[j])
+                        for j in range(K)]
         # advection backward of segment frame j with output gradient g_rho[k] -> g_rho[1 - k]
         self.adv_bwd = {}
         ws_bytes = 0

@@ -116,6 +116,7 @@ struct McParams {
   unsigned* cnt;       // reference mode: sample counts
   CT<T>* gback;        // deterministic mode: back-trace gradient per cell (gathered afterwards)
   CT<T>* gface[3];     // density, non-deterministic: face gradients accumulated by backward 2
+  uint8_t* mask;       // MC_SMOOTH revert mask: written by forward 2, read by backward 1 (optional)
   float dt;            // with gface: the lookup is centred(u) * (-dt)
   Dims d;
   int order, clamp, bm, reference;
@@ -162,9 +163,11 @@ struct McState {
   bool mask[C];
 };
 
+// With ``stored`` the MC_SMOOTH mask is read from p.mask instead of being
+// recomputed from the forward trace's corner extrema.
 template <int C, class T, class S>
 __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x, int y, int z, const S lut[3],
-                                         McState<C, S>& s, S vb[8][C], Tri<S>& tb) {
+                                         McState<C, S>& s, S vb[8][C], Tri<S>& tb, bool stored = false) {
   const S p2x = add_rn(-lut[0], S(x)), p2y = add_rn(-lut[1], S(y)), p2z = add_rn(-lut[2], S(z));
   tb = tri_setup(p2x, p2y, p2z, p.d, p.bm);
   if (p.bm == BORDER && !tb.inside) {
@@ -179,7 +182,8 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
     tri_combine<C>(vb, tb, s.back);
   }
   S mn[C], mx[C];
-  if (p.clamp == NGT_CLAMP_MC_SMOOTH) {
+  const bool recompute = p.clamp == NGT_CLAMP_MC_SMOOTH && !(stored && p.mask);
+  if (recompute) {
     const S p1x = add_rn(lut[0], S(x)), p1y = add_rn(lut[1], S(y)), p1z = add_rn(lut[2], S(z));
     read_minmax<C>(p.data, p1x, p1y, p1z, p.d, p.bm, mn, mx);
   }
@@ -188,7 +192,10 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
     s.fwd[c] = p.fwd[i * C + c];
     const S rho = S(ld(p.data + i * C + c));
     s.corr[c] = add_rn(s.fwd[c], mul_rn(S(0.5), sub_rn(rho, s.back[c])));
-    s.mask[c] = (p.clamp == NGT_CLAMP_MC_SMOOTH) && (s.corr[c] < mn[c] || s.corr[c] > mx[c]);
+    if (recompute)
+      s.mask[c] = s.corr[c] < mn[c] || s.corr[c] > mx[c];
+    else
+      s.mask[c] = p.clamp == NGT_CLAMP_MC_SMOOTH && p.mask[i * C + c] != 0;
     s.res[c] = s.mask[c] ? s.fwd[c] : s.corr[c];
   }
 }
@@ -207,6 +214,7 @@ __device__ __forceinline__ void mc_fwd2_at(const McParams<T>& p, const LK& lk, i
   for (int c = 0; c < C; ++c) {
     const S o = (p.clamp == NGT_CLAMP_NEGATIVE) ? fmax(s.res[c], S(0)) : s.res[c];
     p.out[i * C + c] = from_compute<T>(o);
+    if (p.mask && p.clamp == NGT_CLAMP_MC_SMOOTH) p.mask[i * C + c] = s.mask[c] ? 1 : 0;
   }
 }
 
@@ -264,7 +272,7 @@ __device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, i
     McState<C, S> s;
     S vb[8][C];
     Tri<S> tb;
-    mc_state<C>(p, i, x, y, z, lut, s, vb, tb);
+    mc_state<C>(p, i, x, y, z, lut, s, vb, tb, true);
     S gback[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) {
@@ -611,6 +619,7 @@ McParams<T> density_params(const ngt_advect_args* a) {
   p.data = static_cast<const T*>(a->data);
   p.out = static_cast<T*>(a->output);
   p.fwd = static_cast<CT<T>*>(a->fwd_field);
+  p.mask = static_cast<uint8_t*>(a->mask);
   p.d = cells_of(a->grid_dhw);
   p.order = a->order;
   p.clamp = a->clamp;

@@ -439,16 +439,26 @@ __device__ __forceinline__ void bwd_bl_tile(const RayParams& p, const Cam& cam, 
   }
 }
 
+// The checkpointed adjoint as a call of its own (its registers and stack do not
+// weigh on the one-pass kernel that calls it for launches with a possibly
+// negative extinction sample).
 template <int CIN, int CB, class T, class S>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(RayParams p) {
-  if (*p.flag != 0) return;
+__device__ __noinline__ void bwd_exact_tile_call(const RayParams& p, const Cam& cam, int b, int oslot, int tile) {
+  bwd_exact_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
+}
+
+template <int CIN, int CB, class T, class S>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(const __grid_constant__ RayParams p) {
   __shared__ Cam cam;
   __shared__ CamScratch cam_sh;
   int b, c, oslot;
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
   load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
   __syncthreads();
-  bwd_bl_tile<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
+  if (*p.flag != 0)
+    bwd_exact_tile_call<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
+  else
+    bwd_bl_tile<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
 }
 
 // Sets *flag when some voxel makes a negative extinction sample possible: a
@@ -725,8 +735,7 @@ __global__ void __launch_bounds__(kThreads, CIN == 1 ? 8 : 4) k_raymarch_batch(c
     const int slot = local / bp.tiles_per_slot[it], tile = local - slot * bp.tiles_per_slot[it];
     // the one-pass backward takes scenes with non-negative extinction, the
     // checkpointed one the others
-    const bool run = WHICH == FWD || (WHICH == BWD_BL ? (CB > 1 && bp.flags[it] == 0) : bp.flags[it] != 0);
-    if (!run) continue;
+    const bool checkpointed = WHICH != FWD && bp.flags[it] != 0;
     int b, c, oslot;
     slot_to_bc(p, slot, b, c, oslot);
     const float* src = reinterpret_cast<const float*>(p.cams + slot);
@@ -735,10 +744,10 @@ __global__ void __launch_bounds__(kThreads, CIN == 1 ? 8 : 4) k_raymarch_batch(c
     __syncthreads();
     if (WHICH == FWD)
       fwd_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
-    else if (WHICH == BWD_BL)
-      bwd_bl_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
+    else if (checkpointed || CB == 1)
+      bwd_exact_tile_call<CIN, CB, T, S>(p, cam, b, oslot, tile);
     else
-      bwd_exact_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
+      bwd_bl_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
   }
 }
 
@@ -801,8 +810,6 @@ void launch_batch(int which, unsigned blocks, cudaStream_t st, const RayBatch& b
     k_raymarch_batch<CIN, CB, T, S, FWD><<<blocks, kThreads, 0, st>>>(bp);
   } else if (which == BWD_BL) {
     k_raymarch_batch<CIN, CB, T, S, BWD_BL><<<blocks, kThreads, 0, st>>>(bp);
-  } else if (which == BWD_EXACT) {
-    k_raymarch_batch<CIN, CB, T, S, BWD_EXACT><<<blocks, kThreads, 0, st>>>(bp);
   } else {
     k_extinction_sign_batch<CIN, CB, T><<<dim3(blocks, unsigned(bp.count)), 256, 0, st>>>(bp);
   }
@@ -1049,11 +1056,12 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
         rc = launch_dtype(a->fwd.dtype, SIGN, cin, cb, dim3(1), st, p);
         if (rc) return rc;
       }
-      rc = launch_slots(a->fwd.dtype, BWD_BL, cin, cb, tiles, st, p);
+      rc = launch_slots(a->fwd.dtype, BWD_BL, cin, cb, tiles, st, p);  // one-pass, or checkpointed on the flag
+      if (rc) return rc;
+    } else {
+      rc = launch_slots(a->fwd.dtype, BWD_EXACT, cin, cb, tiles, st, p);
       if (rc) return rc;
     }
-    rc = launch_slots(a->fwd.dtype, BWD_EXACT, cin, cb, tiles, st, p);
-    if (rc) return rc;
     if (quad) {
       CellLaunch fl = cell_launch(p.din);
       fl.grid.z = unsigned(p.din.z * p.N);
@@ -1309,10 +1317,6 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
   if (rc) return rc;
   const unsigned blocks = persistent_blocks(blocks_per_sm, bp.total);
   rc = launch_batch_dtype(dtype, BWD_BL, cin, cb, blocks, st, bp);
-  if (rc) return rc;
-  RayBatch bp2 = bp;
-  bp2.counter += 1;  // second persistent pass: scenes with possibly negative extinction
-  rc = launch_batch_dtype(dtype, BWD_EXACT, cin, cb, blocks, st, bp2);
   if (rc) return rc;
   if (quad) k_quad_fold_batch<<<unsigned(bp.cblock_end[count - 1]), dim3(32, 8), 0, st>>>(bp);
   return check_launch("ngt_raymarch_bwd_batch");

@@ -24,9 +24,10 @@ from .ops import _code, _ptr
 
 class RenderAdvectStep:
     # kernels of one f32 exact Beer-Lambert step: advect fwd 2, raymarch fwd 2 (quad
-    # layout, march), loss 1, raymarch bwd 4 (quad layout with the sign check,
-    # one-pass and checkpointed marches, fold), advect bwd 2
-    KERNELS_PER_STEP = 11
+    # layout, march), loss 1, raymarch bwd 3 (quad layout with the sign check, the
+    # one-pass march -- checkpointed where the sign check fails -- and the fold),
+    # advect bwd 2
+    KERNELS_PER_STEP = 10
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact"):
@@ -66,6 +67,9 @@ class RenderAdvectStep:
         a.data, a.vel_x, a.vel_y, a.vel_z = _ptr(self.rho), _ptr(self.ux), _ptr(self.uy), _ptr(self.uz)
         a.dt, a.order, a.clamp, a.boundary = float(dt), int(order), L.CLAMP[clamp], L.BOUNDARY[advect_boundary]
         a.output, a.fwd_field = _ptr(self.rho_adv), _ptr(self.fwd_field)
+        # the forward's MC_SMOOTH revert mask, read back by the backward
+        self.mc_mask = torch.empty((D, H, W, 1), dtype=torch.uint8, device=dev)
+        a.mask = _ptr(self.mc_mask)
         self.adv = a
         ag = L.AdvectGradArgs()
         ag.fwd = a

@@ -462,3 +462,21 @@ def test_advect_backward_deterministic(bm):
     ref = oadvect.density_maccormack_grad(rho, ux, uy, uz, g, boundary=bm)
     for t, r in zip(grads[0], ref):
         assert rel(r, N(t)) < 1e-4
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
+def test_advect_stored_mask_matches_recomputed(bm):
+    """The backward reading the forward's stored MC_SMOOTH mask equals the
+    backward recomputing it from the corner extrema."""
+    from ngt_gb300 import advect
+    rho, ux, uy, uz = advect_inputs(shape=(12, 14, 16), seed=29)
+    ts = [T(a) for a in (rho, ux, uy, uz)]
+    g = T(RNG.standard_normal(rho.shape).astype(np.float32))
+    out, fwd, mask = advect.warp_forward(*ts, boundary=bm, keep_mask=True)
+    out2, _, _ = advect.warp_forward(*ts, boundary=bm)
+    assert torch.equal(out, out2)
+    assert int(mask.sum()) > 0
+    a = advect.warp_backward(*ts, fwd, g, boundary=bm, mask=mask)
+    b = advect.warp_backward(*ts, fwd, g, boundary=bm)
+    for x, y in zip(a, b):
+        assert rel(N(y), N(x)) < 1e-6
