@@ -171,6 +171,38 @@ __device__ __forceinline__ bool quad_setup(float px, float py, float pz, const D
   return true;
 }
 
+// The raymarch's sample through the quad layout, without the explicit rounding
+// of read_linear_quad: the lerps contract to FMAs (the raymarch matches the
+// oracle to a tolerance, not bit for bit).  Returns false outside (BORDER).
+template <class T>
+__device__ __forceinline__ bool quad_sample_fma(const typename QuadOf<T>::type* __restrict__ q, float px, float py,
+                                                float pz, const Dims& d, const QuadDims& qd, int bm, QuadPos& s,
+                                                float& v) {
+  if (!quad_setup(px, py, pz, d, qd, bm, s)) {
+    v = 0.0f;
+    return false;
+  }
+  float a[4], b[4];
+  quad_fetch<T>(q, s.idx, a);
+  quad_fetch<T>(q, s.idx + qd.plane, b);
+  const float a0 = fmaf(s.w[0], a[1] - a[0], a[0]), a1 = fmaf(s.w[0], a[3] - a[2], a[2]);
+  const float b0 = fmaf(s.w[0], b[1] - b[0], b[0]), b1 = fmaf(s.w[0], b[3] - b[2], b[2]);
+  const float v0 = fmaf(s.w[1], a1 - a0, a0), v1 = fmaf(s.w[1], b1 - b0, b0);
+  v = fmaf(s.w[2], v1 - v0, v0);
+  return true;
+}
+
+// scatter_linear_quad for a position already set up by quad_sample_fma.
+__device__ __forceinline__ void scatter_quad_at(float4* __restrict__ gq, const QuadPos& s, const QuadDims& qd,
+                                                float g) {
+  const float wx1 = s.w[0], wx0 = 1.0f - s.w[0];
+  const float wy1 = s.w[1], wy0 = 1.0f - s.w[1];
+  const float g0 = g * (1.0f - s.w[2]), g1 = g * s.w[2];
+  const float a00 = wx0 * wy0, a10 = wx1 * wy0, a01 = wx0 * wy1, a11 = wx1 * wy1;
+  atomicAdd(gq + s.idx, make_float4(g0 * a00, g0 * a10, g0 * a01, g0 * a11));
+  atomicAdd(gq + s.idx + qd.plane, make_float4(g1 * a00, g1 * a10, g1 * a01, g1 * a11));
+}
+
 template <class T>
 __device__ __forceinline__ float read_linear_quad(const typename QuadOf<T>::type* __restrict__ q, float px, float py,
                                                   float pz, const Dims& d, const QuadDims& qd, int bm) {

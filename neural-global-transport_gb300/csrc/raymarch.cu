@@ -257,6 +257,35 @@ __device__ __forceinline__ void fwd_tile(const RayParams& p, const Cam& cam, int
   S acc[CB];
 #pragma unroll
   for (int k = 0; k < CB; ++k) acc[k] = S(0);
+  if constexpr (quad_able<CIN, T>() && CB > 1) {
+    // emission Beer-Lambert through the quad layout: the step's hot loop
+    if (qg && p.blend == BEER_LAMBERT && r.hit) {
+      const auto* q = static_cast<const typename QuadOf<T>::type*>(qg);
+      float sc[CB];
+#pragma unroll
+      for (int k = 0; k < CB; ++k) sc[k] = p.scale[k];
+      float pos[3] = {r.s[0], r.s[1], r.s[2]};
+      float dd = 0.0f, L[CB - 1];
+#pragma unroll
+      for (int k = 0; k < CB - 1; ++k) L[k] = 0.0f;
+      for (int i = 0; i < r.steps; ++i) {
+        QuadPos qp;
+        float v;
+        quad_sample_fma<T>(q, pos[0] - 0.5f, pos[1] - 0.5f, pos[2] - 0.5f, p.din, p.qd, p.bm, qp, v);
+        dd = fmaxf(dd + sc[CB - 1] * v, 0.0f);
+        const float t = __expf(-dd);
+#pragma unroll
+        for (int k = 0; k < CB - 1; ++k) L[k] += t * (sc[k] * v);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
+      }
+      S* out = reinterpret_cast<S*>(p.output) + ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
+#pragma unroll
+      for (int k = 0; k < CB - 1; ++k) out[k] = L[k];
+      out[CB - 1] = dd;
+      return;
+    }
+  }
   if (r.hit) {
     float pos[3] = {r.s[0], r.s[1], r.s[2]};
     for (int i = 0; i < r.steps; ++i) {
@@ -418,6 +447,33 @@ __device__ __forceinline__ void bwd_bl_tile(const RayParams& p, const Cam& cam, 
 #pragma unroll
   for (int k = 0; k < CB - 1; ++k) lgf += G[k] * reinterpret_cast<const S*>(p.out_fwd)[o + k];
   const S gD = G[CB - 1];
+  if constexpr (quad_able<CIN, T>() && std::is_same<S, float>::value) {
+    if (qg && gq) {
+      // one-channel emission through the quad layout: one set-up per sample for
+      // the gather and the two vector atomics of its adjoint
+      const auto* q = static_cast<const typename QuadOf<T>::type*>(qg);
+      float sg = 0.0f;  // sum_c scale_c * gL_c
+#pragma unroll
+      for (int k = 0; k < CB - 1; ++k) sg += p.scale[k] * G[k];
+      const float sl = p.scale[CB - 1];
+      float dd = 0.0f, w = 0.0f;
+      float pos[3] = {r.s[0], r.s[1], r.s[2]};
+      for (int i = 0; i < r.steps; ++i) {
+        QuadPos qp;
+        float v;
+        const bool in = quad_sample_fma<T>(q, pos[0] - 0.5f, pos[1] - 0.5f, pos[2] - 0.5f, p.din, p.qd, p.bm, qp, v);
+        dd = dd + sl * v;
+        const float t = __expf(-dd);
+        // d rho = sum_c scale_c * t * gL_c + scale_sigma * (gD - (L.gL - W))
+        const float gs = t * sg + sl * (float(gD) - (float(lgf) - w));
+        w += t * (v * sg);
+        if (in) scatter_quad_at(gq, qp, p.qd, gs);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
+      }
+      return;
+    }
+  }
   S d = S(0), w = S(0);
   float pos[3] = {r.s[0], r.s[1], r.s[2]};
   for (int i = 0; i < r.steps; ++i) {
