@@ -70,17 +70,20 @@ __device__ __forceinline__ void quad_build_at(const T* __restrict__ g, const Dim
                                               int yq, int zq, int b) {
   const QuadDims qd = QuadDims::of(d);
   const int64_t e = (int64_t(zq) * qd.y + yq) * qd.x + xq;
-  bool vz;
+  // the two columns, two rows and the plane of this entry, boundary rule applied once each
+  bool vz, vx0, vx1, vy0, vy1;
   const int z = quad_cell(zq - 1, d.z, bm, vz);
+  const int x0 = quad_cell(xq - 1, d.x, bm, vx0), x1 = quad_cell(xq, d.x, bm, vx1);
+  const int y0 = quad_cell(yq - 1, d.y, bm, vy0), y1 = quad_cell(yq, d.y, bm, vy1);
+  const T* plane = g + (int64_t(b) * d.z + z) * (int64_t(d.x) * d.y);
+  const T* r0 = plane + int64_t(y0) * d.x;
+  const T* r1 = plane + int64_t(y1) * d.x;
+  const T zero = T(0.0f);
   T v[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    bool vx, vy;
-    const int x = quad_cell(xq - 1 + (k & 1), d.x, bm, vx);
-    const int y = quad_cell(yq - 1 + (k >> 1), d.y, bm, vy);
-    const T* src = g + int64_t(b) * d.count() + flat(x, y, z, d);
-    v[k] = (vx && vy && vz) ? *src : T(0.0f);
-  }
+  v[0] = (vz && vy0 && vx0) ? r0[x0] : zero;
+  v[1] = (vz && vy0 && vx1) ? r0[x1] : zero;
+  v[2] = (vz && vy1 && vx0) ? r1[x0] : zero;
+  v[3] = (vz && vy1 && vx1) ? r1[x1] : zero;
   if (neg) {
     bool n = false;
 #pragma unroll
