@@ -411,11 +411,35 @@ def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params,
     return _RaymarchGridTransform.apply(input, M, V, P, F, out_dhw, attrs)
 
 
+class _RaymarchGridTransformGrad(torch.autograd.Function):
+    """The gradient op used as a forward op (the renderer's unprojection of images
+    into the volume), differentiable w.r.t. ``output_grad`` as registered in
+    ops_loader.py:98-118: for ADDITIVE blending its gradient is the forward
+    raymarch of the incoming volume gradient; input and output get none."""
+
+    @staticmethod
+    def forward(ctx, input, output, output_grad, M, V, P, F, out_dhw, attrs, mode):
+        ctx.geom = (M, V, P, F, out_dhw, attrs, output_grad.shape)
+        return _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, attrs, mode)
+
+    @staticmethod
+    def backward(ctx, grad):
+        M, V, P, F, out_dhw, attrs, shape = ctx.geom
+        blend = attrs["blending_mode"]
+        blend = blend.decode() if isinstance(blend, bytes) else blend
+        if blend != "ADDITIVE":
+            raise NotImplementedError("Gradient of raymach op gradient only available for ADDITIVE blending, is %s"
+                                      % blend)
+        gg = _ray_forward(grad.contiguous(), M, V, P, F, out_dhw, dict(attrs, emission_scale=None))
+        return None, None, gg.reshape(shape), None, None, None, None, None, None, None
+
+
 def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,
                                  output_shape, interpolation="LINEAR", boundary="BORDER",
                                  blending_mode="BEER_LAMBERT", keep_dims=False, separate_camera_batch=True,
                                  grad_mode=None, emission_scale=None):
-    """``RaymarchGridTransformGrad`` (raymarch_grid.cc:67-92): the input gradient."""
+    """``RaymarchGridTransformGrad`` (raymarch_grid.cc:67-92): the input gradient.
+    Differentiable w.r.t. ``output_grad`` for ADDITIVE blending (ops_loader.py:98-118)."""
     input = _cuda(input, "input")
     dev = input.device
     M, V, P, F = (_floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev),
@@ -424,8 +448,29 @@ def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v,
                  separate_camera_batch=separate_camera_batch,
                  emission_scale=None if emission_scale is None else tuple(float(v) for v in emission_scale))
     cd = compute_dtype(input)
-    return _ray_backward(input, _cuda(output, "output").to(cd), _cuda(output_grad, "output_grad").to(cd), M, V, P, F,
-                         tuple(int(s) for s in list(output_shape)[:3]), attrs, grad_mode or get_gradient_mode())
+    return _RaymarchGridTransformGrad.apply(input, _cuda(output, "output").to(cd),
+                                            _cuda(output_grad, "output_grad").to(cd), M, V, P, F,
+                                            tuple(int(s) for s in list(output_shape)[:3]), attrs,
+                                            grad_mode or get_gradient_mode())
+
+
+def unproject(images, matrix_m, matrix_v, matrix_p, frustum_params, grid_dhw, depth, interpolation="LINEAR",
+              boundary="BORDER", separate_camera_batch=True, grad_mode="reference"):
+    """Scatter images back into the volume along the camera rays, as
+    ``Renderer._raymarch_camera_transform(inverse=True)`` does (renderer.py:372-398):
+    the ADDITIVE raymarch gradient op with the images as output gradient and a zero
+    volume, ``depth`` samples per ray.  ``images``: N, V, H, W, C.  The reference op
+    normalises each camera's scatter by its summed sample weights
+    (``grad_mode='reference'``); ``'exact'`` gives the plain adjoint.
+    Differentiable w.r.t. the images (the forward raymarch)."""
+    images = _cuda(images, "images")
+    N, H, W, C = images.shape[0], images.shape[2], images.shape[3], images.shape[4]
+    D0, H0, W0 = (int(v) for v in grid_dhw)
+    dummy = torch.zeros((N, D0, H0, W0, C), dtype=images.dtype, device=images.device)
+    return raymarch_grid_transform_grad(dummy, images, images, matrix_m, matrix_v, matrix_p, frustum_params,
+                                        (int(depth), H, W), interpolation=interpolation, boundary=boundary,
+                                        blending_mode="ADDITIVE", separate_camera_batch=separate_camera_batch,
+                                        grad_mode=grad_mode)
 
 
 # -------------------------------------------------------------- reduce blend

@@ -483,3 +483,23 @@ def test_advect_stored_mask_matches_recomputed(bm):
     b = advect.warp_backward(*ts, fwd, g, boundary=bm)
     for x, y in zip(a, b):
         assert rel(N(y), N(x)) < 1e-6
+
+
+# ------------------------------------------------------------- unprojection
+@pytest.mark.parametrize("mode", ["reference", "exact"])
+def test_unproject_and_its_gradient(mode):
+    """Images scattered into the volume by the ADDITIVE gradient op (renderer.py:372-398)
+    match the oracle; its registered gradient w.r.t. the images is the forward
+    raymarch of the volume gradient (ops_loader.py:98-118)."""
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    img = RNG.uniform(0, 1, (1, 3, 8, 6, 2)).astype(np.float32)
+    it = T(img).requires_grad_()
+    vol = ngt().unproject(it, M, V, P, F, (10, 12, 14), 10, grad_mode=mode)
+    dummy = np.zeros((1, 10, 12, 14, 2), np.float32)
+    ref = oops.raymarch_grid_transform_grad(dummy, img, img, M, V, P, F, [10, 8, 6], "LINEAR", "BORDER", "ADDITIVE",
+                                            grad_mode=mode)
+    assert rel(ref, N(vol)) < (5e-4 if mode == "reference" else 1e-4)
+    wv = RNG.standard_normal(ref.shape).astype(np.float32)
+    (vol * T(wv)).sum().backward()
+    want = oops.raymarch_grid_transform(wv, M, V, P, F, [10, 8, 6], "LINEAR", "BORDER", "ADDITIVE")
+    assert rel(want, N(it.grad)) < 2e-5
