@@ -323,7 +323,7 @@ __device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, i
 }
 
 template <int C, class T, class LK>
-__global__ void __launch_bounds__(kBlock) k_mc_bwd1(McParams<T> p, LK lk) {
+__global__ void __launch_bounds__(kBlock, 5) k_mc_bwd1(McParams<T> p, LK lk) {
   int x, y, z;
   const bool active = launch_cell(p.d, x, y, z);
   if (__all_sync(0xffffffffu, !active)) return;
@@ -389,16 +389,20 @@ __device__ __forceinline__ void mc_bwd2_at(const McParams<T>& p, const LK& lk, i
   S g[C];
 #pragma unroll
   for (int c = 0; c < C; ++c) g[c] = p.gfwd[i * C + c];
+  const Tri<S> t = tri_setup(p1x, p1y, p1z, p.d, p.bm);
   if (p.det) {
   } else if (p.reference) {
     if (active) scatter_linear_counted<C>(p.buf, p.cnt, p1x, p1y, p1z, p.d, p.bm, g);
   } else {
-    scatter_linear_warp<C>(p.gdata, p1x, p1y, p1z, p.d, p.bm, g, active);
+    scatter_linear_warp<C>(p.gdata, t, p.d, p.bm, g, active);
   }
-  if (!active) return;
-  const Tri<S> t = tri_setup(p1x, p1y, p1z, p.d, p.bm);
-  S gl[3] = {p.glut[i * 3 + 0], p.glut[i * 3 + 1], p.glut[i * 3 + 2]};
-  if (!(p.bm == BORDER && !t.inside)) {
+  S gl[3] = {S(0), S(0), S(0)};
+  if (active) {
+    gl[0] = p.glut[i * 3 + 0];
+    gl[1] = p.glut[i * 3 + 1];
+    gl[2] = p.glut[i * 3 + 2];
+  }
+  if (active && !(p.bm == BORDER && !t.inside)) {
     S v[8][C], dx[C], dy[C], dz[C];
     tri_fetch<C>(p.data, t, p.d, v);
     tri_gradient<C>(v, t, dx, dy, dz);
@@ -413,17 +417,25 @@ __device__ __forceinline__ void mc_bwd2_at(const McParams<T>& p, const LK& lk, i
   if (p.gface[0]) {
     const S h = S(-0.5) * S(p.dt);
     const S gx = gl[0] * h, gy = gl[1] * h, gz = gl[2] * h;
+    // x faces: face x gets this cell's and the previous cell's share; lanes hold
+    // consecutive cells of one row, so the previous lane's share comes by shuffle
+    // and only the first lane of the warp and the row's last cell add to a second face
+    const int lane = threadIdx.x & 31;
+    const S gprev = __shfl_up_sync(0xffffffffu, gx, 1);
+    const bool merged = lane > 0;  // padding lanes carry gx = 0 (gl = 0)
+    if (!active) return;
     S* fx = p.gface[0] + (int64_t(z) * p.d.y + y) * (p.d.x + 1) + x;
     S* fy = p.gface[1] + (int64_t(z) * (p.d.y + 1) + y) * p.d.x + x;
     S* fz = p.gface[2] + (int64_t(z) * p.d.y + y) * p.d.x + x;
-    atomic_add(fx, gx);
-    atomic_add(fx + 1, gx);
+    atomic_add(fx, merged ? gx + gprev : gx);
+    if (lane == 31 || x == p.d.x - 1) atomic_add(fx + 1, gx);
     atomic_add(fy, gy);
     atomic_add(fy + p.d.x, gy);
     atomic_add(fz, gz);
     atomic_add(fz + int64_t(p.d.x) * p.d.y, gz);
     return;
   }
+  if (!active) return;
   p.glut[i * 3 + 0] = gl[0];
   p.glut[i * 3 + 1] = gl[1];
   p.glut[i * 3 + 2] = gl[2];

@@ -335,11 +335,10 @@ __device__ __forceinline__ void read_minmax(const T* __restrict__ g, S px, S py,
 // to its own before the atomics, so neighbouring samples share one atomic per
 // corner.  Same sums as scatter_linear up to the order of the additions.
 template <int C, class S>
-__device__ __forceinline__ void scatter_linear_warp(S* __restrict__ grad, S px, S py, S pz, const Dims& d, int bm,
+__device__ __forceinline__ void scatter_linear_warp(S* __restrict__ grad, const Tri<S>& t, const Dims& d, int bm,
                                                     const S g[C], bool active) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const Tri<S> t = tri_setup(px, py, pz, d, bm);
   const bool on = active && !(bm == BORDER && !t.inside);
   // corner values: lo[j] at x = i0x, hi[j] at x = i1x, j = (y, z) in reference order
   S lo[4][C], hi[4][C];
@@ -385,6 +384,12 @@ __device__ __forceinline__ void scatter_linear_warp(S* __restrict__ grad, S px, 
       }
     }
   }
+}
+
+template <int C, class S>
+__device__ __forceinline__ void scatter_linear_warp(S* __restrict__ grad, S px, S py, S pz, const Dims& d, int bm,
+                                                    const S g[C], bool active) {
+  scatter_linear_warp<C>(grad, tri_setup(px, py, pz, d, bm), d, bm, g, active);
 }
 
 // Quadratic B-spline weight (sampling.hpp:247-256)
