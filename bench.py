@@ -292,6 +292,7 @@ def gpu_arm(args, world, rank, local):
         kernel = kernel_stats(step, torch, dev, w, st, max(10, args.steps // 2), flush)
 
     e2e = e2e_measure(torch, dev, w, st, tgt, args, flush)
+    e2e_step = e2e_step_measure(torch, step, w, st, args, flush) if not args.no_graph else None
     samples = 2 * 2 * 128 ** 3 + 2 * 5 * 256 * 256 * 128
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -318,6 +319,8 @@ def gpu_arm(args, world, rank, local):
     if clk:
         line["clocks"] = clk
     line["e2e"] = e2e
+    if e2e_step:
+        line["e2e_step"] = e2e_step
     if rank == 0 and world == 1 and args.cpu_baseline == "on":
         t, sample = cpu_step_time(1, adv_n=48, rows=4)
         line["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": 1, "kind": "port",
@@ -398,6 +401,34 @@ def e2e_measure(torch, dev, w, st, tgt, args, flush):
         tot += time.perf_counter() - t0
     return {"value": n / tot, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
             "path": "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + torch loss.backward()"}
+
+
+def e2e_step_measure(torch, step, w, st, args, flush):
+    """The fused step's public call (``RenderAdvectStep.step``, one CUDA graph)
+    end to end: density and velocity copied from pinned host memory into the
+    step's inputs every step, the loss read back."""
+    host = [torch.as_tensor(a).to(st).pin_memory() for a in (w.rho, w.ux, w.uy, w.uz)]
+    dst = [step.rho, step.ux, step.uy, step.uz]
+    h2d = sum(t.numel() * t.element_size() for t in host)
+
+    def one():
+        for d, h in zip(dst, host):
+            d.copy_(h, non_blocking=True)
+        return float(step.step().item())
+
+    for _ in range(max(2, args.warmup)):
+        one()
+    torch.cuda.synchronize()
+    n = max(5, args.steps // 2)
+    tot = 0.0
+    for _ in range(n):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        one()
+        tot += time.perf_counter() - t0
+    return {"value": n / tot, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
+            "path": "ngt_gb300.step.RenderAdvectStep.step (one CUDA graph)"}
 
 
 # ------------------------------------------------------------ other workloads

@@ -91,11 +91,16 @@ def _enum(table, value, name):
 
 def _floats(m, width, device):
     """Matrices / frusta as the contiguous float32 device buffer the kernels read:
-    the C-order flattening of what the caller passed, ``width`` floats per entry."""
+    the C-order flattening of what the caller passed, ``width`` floats per entry.
+
+    Host arrays go through pinned staging memory with a stream-ordered copy: a copy
+    from pageable memory would first wait for all work queued on the stream, so
+    every call taking numpy matrices would stall the host behind the GPU."""
     if isinstance(m, torch.Tensor):
-        t = m.detach().to(device=device, dtype=torch.float32)
+        t = m.detach().to(device=device, dtype=torch.float32, non_blocking=True)
     else:
-        t = torch.as_tensor(np.asarray(m, dtype=np.float32), device=device)
+        host = torch.from_numpy(np.ascontiguousarray(m, dtype=np.float32))
+        t = host.pin_memory().to(device=device, non_blocking=True)
     return t.reshape(-1, width).contiguous()
 
 

@@ -61,6 +61,35 @@ class Transform:
         return np.linalg.inv(self.get_transform_matrix())
 
 
+class MatrixTransform:
+    """A transform given by its 4x4 matrix (``MatrixTransform``, transform.py:11-39);
+    ``grid_size`` (D, H, W) is carried for cameras whose frustum grid it sets."""
+
+    def __init__(self, matrix=None, parent=None, grid_size=None):
+        self.matrix = np.eye(4) if matrix is None else np.asarray(matrix, dtype=np.float64)
+        self.parent = parent
+        self.grid_size = None if grid_size is None else [int(s) for s in grid_size]
+
+    @classmethod
+    def from_fwd_up_right_pos(cls, fwd, up, right, pos, parent=None):
+        """Columns right, up, forward and the position (transform.py:32-39)."""
+        m = np.eye(4)
+        m[:3, 0], m[:3, 1], m[:3, 2], m[:3, 3] = right, up, fwd, pos
+        return cls(m, parent)
+
+    def get_local_transform(self):
+        return self.matrix
+
+    def get_transform_matrix(self):
+        m = self.get_local_transform()
+        if self.parent is not None:
+            return self.parent.get_transform_matrix() @ m
+        return m
+
+    def get_inverse_transform(self):
+        return np.linalg.inv(self.get_transform_matrix())
+
+
 class GridTransform(Transform):
     """A grid of shape ``grid_size`` (D, H, W) placed in world space."""
 
@@ -83,6 +112,12 @@ class GridTransform(Transform):
         elif self.normalize == "MAX":
             m = scale_matrix([1.0 / size.max()] * 3) @ m
         return translation_matrix(self.translation) @ (rotation_matrix_xyz_deg(self.rotation_deg) @ m)
+
+    def grid_size_world(self):
+        """World-space lengths of the grid's x, y and z edges (transform.py:390-395)."""
+        m = self.get_transform_matrix()
+        size = np.asarray(self.grid_size[::-1], dtype=np.float64)
+        return np.linalg.norm(m[:3, :3] * size[None, :], axis=0)
 
 
 class Camera:
