@@ -204,6 +204,12 @@ typedef struct {
    * ngt_raymarch_cameras for these matrices (static cameras across calls).
    * Null: formed on every call.  Used by forward and backward. */
   const void* cameras;
+  /* Optional: this input in the quad gather layout, prepared by
+   * ngt_raymarch_quad (one-channel LINEAR input in float or 16-bit storage)
+   * and valid while the input is unchanged.  Forward and exact backward read it
+   * instead of building their own.  Null: built per call.  The batch entry
+   * points build their own and reject it. */
+  const void* quad;
 } ngt_raymarch_args;
 
 typedef struct {
@@ -228,6 +234,18 @@ size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* args);
 size_t ngt_raymarch_cameras_bytes(const ngt_raymarch_args* args);
 int ngt_raymarch_cameras(const ngt_raymarch_args* args, void* cameras, void* stream);
 int ngt_raymarch_fwd(const ngt_raymarch_args* args, void* stream);
+/* The quad gather layout of args' input (each cell's 2x2 (x, y) neighbours per z
+ * slab, the boundary rule applied), prepared once for the forward and the
+ * backward of the same input, which then skip their own builds; it holds the
+ * extinction-sign word of the one-pass Beer-Lambert adjoint, taken with args'
+ * emission scale.  ``quad``: device memory of ngt_raymarch_quad_bytes bytes,
+ * 256-byte aligned.  ngt_raymarch_quad_bytes is 0 for inputs the layout does
+ * not serve (several channels, NEAREST / MIN / MAX, F64), for which
+ * ngt_raymarch_quad fails with NGT_ERR_UNSUPPORTED.  No counterpart in the
+ * reference, whose kernels gather the eight corners per sample
+ * (sampling_v2.hpp:37-124). */
+size_t ngt_raymarch_quad_bytes(const ngt_raymarch_args* args);
+int ngt_raymarch_quad(const ngt_raymarch_args* args, void* quad, void* stream);
 int ngt_raymarch_bwd(const ngt_raymarch_grad_args* args, void* stream);
 size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* args);
 /* ngt_raymarch_bwd for callers that cannot allocate device memory -- a host

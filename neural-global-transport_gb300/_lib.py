@@ -63,7 +63,7 @@ class RaymarchArgs(ctypes.Structure):
                 ("num_cameras", c_i32), ("output", c_vp), ("interpolation", c_i32), ("boundary", c_i32),
                 ("blending_mode", c_i32), ("keep_dims", c_i32), ("separate_camera_batch", c_i32),
                 ("emission_channels", c_i32), ("emission_scale", c_f32 * 4), ("workspace", c_vp),
-                ("workspace_bytes", c_sz), ("cameras", c_vp)]
+                ("workspace_bytes", c_sz), ("cameras", c_vp), ("quad", c_vp)]
 
 
 class RaymarchGradArgs(ctypes.Structure):
@@ -121,6 +121,8 @@ SIGNATURES = {
     "ngt_raymarch_fwd_workspace_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
     "ngt_raymarch_cameras_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
     "ngt_raymarch_cameras": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp], c_i32),
+    "ngt_raymarch_quad_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
+    "ngt_raymarch_quad": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp], c_i32),
     "ngt_raymarch_fwd": ([ctypes.POINTER(RaymarchArgs), c_vp], c_i32),
     "ngt_raymarch_bwd": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
     "ngt_raymarch_bwd_workspace_bytes": ([ctypes.POINTER(RaymarchGradArgs)], c_sz),

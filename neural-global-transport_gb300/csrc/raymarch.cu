@@ -926,6 +926,16 @@ bool needs_sign_flag(const ngt_raymarch_grad_args* a) {
   return a->grad_mode == NGT_GRAD_EXACT && a->fwd.blending_mode == NGT_BEER_LAMBERT && cb > 1;
 }
 
+// A prepared quad layout: [extinction-sign word, 256 bytes][quad input].
+constexpr size_t kQuadHeader = 256;
+
+int check_prepared_quad(const ngt_raymarch_args* a) {
+  if (a->quad && !quad_case(a))
+    return fail(NGT_ERR_INVALID_ARGUMENT,
+                "raymarch: a prepared quad layout serves one-channel LINEAR inputs in float or 16-bit storage");
+  return NGT_OK;
+}
+
 // Workspace layouts (offsets in bytes, 256-aligned).
 //   forward:            [cameras][quad input]
 //   backward, exact:    [sign flag 256][cameras][quad input][quad gradient]
@@ -938,7 +948,7 @@ Layout fwd_layout(const ngt_raymarch_args* a) {
   Layout l = {};
   l.cams = 0;
   l.quad = cams_bytes(a);
-  l.total = l.quad + (quad_case(a) ? quad_bytes(a) : 0);
+  l.total = l.quad + (quad_case(a) && !a->quad ? quad_bytes(a) : 0);
   return l;
 }
 
@@ -956,7 +966,7 @@ Layout bwd_layout(const ngt_raymarch_grad_args* g) {
   l.flag = 0;
   l.cams = 256;
   l.quad = l.cams + cams_bytes(a);
-  l.gquad = l.quad + (quad_case(a) ? quad_bytes(a) : 0);
+  l.gquad = l.quad + (quad_case(a) && !a->quad ? quad_bytes(a) : 0);
   l.total = l.gquad + (quad_case(a) ? gquad_bytes(a) : 0);
   return l;
 }
@@ -1024,6 +1034,28 @@ extern "C" int ngt_raymarch_cameras(const ngt_raymarch_args* a, void* cameras, v
   return check_launch("ngt_raymarch_cameras");
 }
 
+extern "C" size_t ngt_raymarch_quad_bytes(const ngt_raymarch_args* a) {
+  return a && quad_case(a) ? kQuadHeader + quad_bytes(a) : 0;
+}
+
+extern "C" int ngt_raymarch_quad(const ngt_raymarch_args* a, void* quad, void* stream) {
+  int cin, cb;
+  const int rc = validate(a, cin, cb);
+  if (rc) return rc;
+  if (!quad_case(a))
+    return fail(NGT_ERR_UNSUPPORTED,
+                "raymarch_quad: the quad layout serves one-channel LINEAR inputs in float or 16-bit storage");
+  if (!quad || (reinterpret_cast<uintptr_t>(quad) & 255))
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_quad: null or not 256-byte aligned output");
+  cudaStream_t st = as_stream(stream);
+  char* q = static_cast<char*>(quad);
+  if (cudaMemsetAsync(q, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_quad memset");
+  const float scale = cb > 1 ? a->emission_scale[cb - 1] : 1.0f;
+  const int r = build_quad(a, q + kQuadHeader, st, reinterpret_cast<int*>(q), scale);
+  if (r) return r;
+  return check_launch("ngt_raymarch_quad");
+}
+
 extern "C" size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* a) {
   return a ? fwd_layout(a).total : 0;
 }
@@ -1037,15 +1069,20 @@ extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
   if (rc) return rc;
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null output");
   RayParams p = make_params(a);
+  if ((rc = check_prepared_quad(a))) return rc;
   cudaStream_t st = as_stream(stream);
   if (a->cameras) p.cams = static_cast<const Cam*>(a->cameras);
+  if (a->quad) {
+    p.quad = static_cast<const char*>(a->quad) + kQuadHeader;
+    p.qd = QuadDims::of(p.din);
+  }
   if (a->workspace) {
     const Layout l = fwd_layout(a);
     if (a->workspace_bytes < l.total)
       return fail(NGT_ERR_WORKSPACE, "raymarch: the forward workspace needs %zu bytes", l.total);
     char* w = static_cast<char*>(a->workspace);
     build_cams(p, a, w + l.cams, st);
-    if (quad_case(a)) {
+    if (quad_case(a) && !a->quad) {
       rc = build_quad(a, w + l.quad, st);
       if (rc) return rc;
       p.quad = w + l.quad;
@@ -1073,6 +1110,7 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: invalid grad_mode");
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: the forward output is required");
+  if ((rc = check_prepared_quad(&a->fwd))) return rc;
   const Layout l = bwd_layout(a);
   if (!a->workspace || a->workspace_bytes < l.total)
     return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: needs %zu workspace bytes", l.total);
@@ -1090,16 +1128,26 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   if (a->grad_mode == NGT_GRAD_EXACT) {
     const bool quad = quad_case(&a->fwd);
     const bool bl = needs_sign_flag(a);
+    const bool prepared = quad && a->fwd.quad;
     if (bl) {
-      p.flag = reinterpret_cast<const int*>(w + l.flag);
-      if (cudaMemsetAsync(w + l.flag, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_bwd memset");
+      if (prepared) {
+        p.flag = static_cast<const int*>(a->fwd.quad);  // the prepared layout's sign word
+      } else {
+        p.flag = reinterpret_cast<const int*>(w + l.flag);
+        if (cudaMemsetAsync(w + l.flag, 0, sizeof(int), st) != cudaSuccess)
+          return check_launch("raymarch_bwd memset");
+      }
     }
     if (quad) {
-      // one channel: the quad build also checks the sign of scale * density
-      rc = build_quad(&a->fwd, w + l.quad, st, bl ? reinterpret_cast<int*>(w + l.flag) : nullptr,
-                      cb > 1 ? p.scale[cb - 1] : 1.0f);
-      if (rc) return rc;
-      p.quad = w + l.quad;
+      if (prepared) {
+        p.quad = static_cast<const char*>(a->fwd.quad) + kQuadHeader;
+      } else {
+        // one channel: the quad build also checks the sign of scale * density
+        rc = build_quad(&a->fwd, w + l.quad, st, bl ? reinterpret_cast<int*>(w + l.flag) : nullptr,
+                        cb > 1 ? p.scale[cb - 1] : 1.0f);
+        if (rc) return rc;
+        p.quad = w + l.quad;
+      }
       p.gquad = reinterpret_cast<float4*>(w + l.gquad);
       p.qd = QuadDims::of(p.din);
       if (cudaMemsetAsync(p.gquad, 0, gquad_bytes(&a->fwd), st) != cudaSuccess)
@@ -1314,6 +1362,7 @@ extern "C" int ngt_raymarch_fwd_batch(const ngt_raymarch_args* items, int32_t co
   for (int i = 0; i < count; ++i) {
     ptrs[i] = items + i;
     if (!items[i].output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null output");
+    if (items[i].quad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: builds its own quad layouts");
   }
   cudaStream_t st = as_stream(stream);
   RayBatch bp;
@@ -1338,6 +1387,7 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
   for (int i = 0; i < count; ++i) {
     const ngt_raymarch_grad_args& g = items[i];
     if (!g.output || !g.output_grad || !g.input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null pointer");
+    if (g.fwd.quad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: builds its own quad layouts");
     if (g.grad_mode != NGT_GRAD_EXACT || g.fwd.blending_mode != NGT_BEER_LAMBERT || g.fwd.interpolation != NGT_LINEAR)
       return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: exact Beer-Lambert gradients of LINEAR sampling");
     ptrs[i] = &g.fwd;

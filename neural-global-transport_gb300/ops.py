@@ -360,18 +360,32 @@ def _ray_out_shape(input, V, out_dhw, a):
     return shape if not a["keep_dims"] else (N, nv, 1) + shape[2:]
 
 
-def _ray_forward(input, M, V, P, F, out_dhw, a):
+def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
+    """The forward raymarch: (output, quad).  With ``keep_quad`` an input the
+    quad gather layout serves is prepared into a buffer of its own, returned as
+    ``quad`` for the backward to reuse instead of building it again; otherwise
+    ``quad`` is None."""
     out = torch.empty(_ray_out_shape(input, V, out_dhw, a), dtype=compute_dtype(input), device=input.device)
     r = _ray_args(input, M, V, P, F, out_dhw, out, a)
-    ws = _workspace(L.load().ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r)), input.device)
+    lib = L.load()
+    quad = None
+    if keep_quad:
+        nq = int(lib.ngt_raymarch_quad_bytes(ctypes.byref(r)))
+        if nq:
+            quad = torch.empty(nq, dtype=torch.uint8, device=input.device)
+            L.call("ngt_raymarch_quad", ctypes.byref(r), _ptr(quad), _stream())
+            r.quad = _ptr(quad)
+    ws = _workspace(lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r)), input.device)
     r.workspace, r.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
     L.call("ngt_raymarch_fwd", ctypes.byref(r), _stream())
-    return out
+    return out, quad
 
 
-def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode):
+def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode, quad=None):
     g = L.RaymarchGradArgs()
     g.fwd = _ray_args(input, M, V, P, F, out_dhw, None, a)
+    if quad is not None and mode == "exact":
+        g.fwd.quad = _ptr(quad)
     gi = torch.empty(input.shape, dtype=compute_dtype(input), device=input.device)
     g.output, g.output_grad, g.input_grad, g.grad_mode = _ptr(output), _ptr(output_grad), _ptr(gi), L.GRAD[mode]
     ws = _workspace(L.load().ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g)), input.device)
@@ -383,15 +397,20 @@ def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode):
 class _RaymarchGridTransform(torch.autograd.Function):
     @staticmethod
     def forward(ctx, input, M, V, P, F, out_dhw, attrs):
-        out = _ray_forward(input, M, V, P, F, out_dhw, attrs)
+        mode = get_gradient_mode()
+        # the quad layout built for the forward is kept for an exact backward
+        out, quad = _ray_forward(input, M, V, P, F, out_dhw, attrs,
+                                 keep_quad=ctx.needs_input_grad[0] and mode == "exact")
         ctx.save_for_backward(input, M, V, P, F, out)
-        ctx.attrs, ctx.out_dhw, ctx.mode = attrs, out_dhw, get_gradient_mode()
+        ctx.attrs, ctx.out_dhw, ctx.mode, ctx.quad = attrs, out_dhw, mode, quad
         return out
 
     @staticmethod
     def backward(ctx, grad):
         input, M, V, P, F, out = ctx.saved_tensors
-        gi = _ray_backward(input, out, grad.contiguous().to(out.dtype), M, V, P, F, ctx.out_dhw, ctx.attrs, ctx.mode)
+        gi = _ray_backward(input, out, grad.contiguous().to(out.dtype), M, V, P, F, ctx.out_dhw, ctx.attrs, ctx.mode,
+                           quad=ctx.quad)
+        ctx.quad = None
         return gi, None, None, None, None, None, None
 
 
@@ -435,7 +454,7 @@ class _RaymarchGridTransformGrad(torch.autograd.Function):
         if blend != "ADDITIVE":
             raise NotImplementedError("Gradient of raymach op gradient only available for ADDITIVE blending, is %s"
                                       % blend)
-        gg = _ray_forward(grad.contiguous(), M, V, P, F, out_dhw, dict(attrs, emission_scale=None))
+        gg, _ = _ray_forward(grad.contiguous(), M, V, P, F, out_dhw, dict(attrs, emission_scale=None))
         return None, None, gg.reshape(shape), None, None, None, None, None, None, None
 
 

@@ -23,11 +23,12 @@ from .ops import _code, _ptr
 
 
 class RenderAdvectStep:
-    # kernels of one f32 exact Beer-Lambert step: advect fwd 2, raymarch fwd 2 (quad
-    # layout, march), loss 1, raymarch bwd 3 (quad layout with the sign check, the
+    # kernels of one f32 exact Beer-Lambert step: advect fwd 2, the quad layout of
+    # the advected density with its extinction-sign check (shared by the render's
+    # forward and backward) 1, raymarch fwd 1, loss 1, raymarch bwd 2 (the
     # one-pass march -- checkpointed where the sign check fails -- and the fold),
     # advect bwd 2
-    KERNELS_PER_STEP = 10
+    KERNELS_PER_STEP = 9
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact"):
@@ -92,6 +93,12 @@ class RenderAdvectStep:
         r.blending_mode, r.keep_dims, r.separate_camera_batch = L.BLEND["BEER_LAMBERT"], 0, 1
         r.emission_channels = 2
         r.emission_scale[0], r.emission_scale[1] = self.emission
+        # the advected density in the quad gather layout, prepared once per step for
+        # the render's forward and backward
+        nq = int(self.lib.ngt_raymarch_quad_bytes(ctypes.byref(r)))
+        self.ray_quad = torch.empty(nq, dtype=torch.uint8, device=dev) if nq else None
+        if nq:
+            r.quad = _ptr(self.ray_quad)
         self.ray_fws = torch.empty(int(self.lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))),
                                    dtype=torch.uint8, device=dev)
         r.workspace, r.workspace_bytes = _ptr(self.ray_fws), self.ray_fws.numel()
@@ -122,6 +129,8 @@ class RenderAdvectStep:
     def forward(self, stream=None):
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream if stream is None else stream)
         self._call("ngt_advect_maccormack_fwd", ctypes.byref(self.adv), s)
+        if self.ray_quad is not None:
+            self._call("ngt_raymarch_quad", ctypes.byref(self.ray), _ptr(self.ray_quad), s)
         self._call("ngt_raymarch_fwd", ctypes.byref(self.ray), s)
 
     def launch(self):

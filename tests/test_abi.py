@@ -138,3 +138,38 @@ def test_workspace_queries(lib):
     assert lib.ngt_sample_lut_bwd_workspace_bytes(ctypes.byref(g)) == 2 * 4 * 5 * 6 * 4
     shape = L.I64x5(1, 8, 8, 8, 2)
     assert lib.ngt_mip_bytes(L.F32, shape, 2) == 4 * 4 * 4 * 2 * 4 + 256  # 512 B level 1, 64 B -> 256 level 2
+
+
+def test_prepared_quad_validation(lib):
+    """The prepared quad layout: sized only for inputs it serves, rejected for
+    the others, for misaligned buffers and by the batch entry points -- all
+    before any device work."""
+    from ngt_gb300 import _lib as L
+    r = L.RaymarchArgs()
+    r.dtype = L.F32
+    r.input_shape = L.I64x5(1, 6, 5, 4, 1)
+    r.output_dhw = L.I64x3(4, 4, 4)
+    for f in ("input", "output", "matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(r, f, ctypes.c_void_p(0x1000))
+    r.num_cameras = 1
+    r.interpolation, r.boundary, r.blending_mode, r.separate_camera_batch = 1, 0, 0, 1
+    # (W+1)(H+1)(D+2) entries of four floats after a 256-byte sign word
+    n = 256 + ((5 * 6 * 8 * 16 + 255) // 256) * 256
+    assert lib.ngt_raymarch_quad_bytes(ctypes.byref(r)) == n
+    assert lib.ngt_raymarch_quad(ctypes.byref(r), ctypes.c_void_p(0x1010), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_raymarch_quad(ctypes.byref(r), None, None) == L.NGT_ERR_INVALID_ARGUMENT
+    r.quad = ctypes.c_void_p(0x1000)
+    assert lib.ngt_raymarch_fwd_batch(ctypes.byref(r), 1, 0, ctypes.c_void_p(0x1000), 1 << 20,
+                                      None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"own quad" in lib.ngt_last_error_message()
+    r.quad = None
+    for field, value in (("input_shape", L.I64x5(1, 6, 5, 4, 2)), ("interpolation", 0), ("dtype", L.F64)):
+        old = getattr(r, field)
+        setattr(r, field, value)
+        assert lib.ngt_raymarch_quad_bytes(ctypes.byref(r)) == 0
+        assert lib.ngt_raymarch_quad(ctypes.byref(r), ctypes.c_void_p(0x1000), None) == L.NGT_ERR_UNSUPPORTED
+        r.quad = ctypes.c_void_p(0x1000)  # a forward given one where it does not apply
+        assert lib.ngt_raymarch_fwd(ctypes.byref(r), None) == L.NGT_ERR_INVALID_ARGUMENT
+        assert b"prepared quad" in lib.ngt_last_error_message()
+        r.quad = None
+        setattr(r, field, old)

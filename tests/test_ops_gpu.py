@@ -288,6 +288,79 @@ def test_raymarch_quad_layout(dtype, bm, blend):
     assert rel(rx, N(gx)) < 1e-4
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
+@pytest.mark.parametrize("signed", [False, True])
+def test_raymarch_prepared_quad(dtype, bm, signed):
+    """A quad layout prepared once (ngt_raymarch_quad) and handed to the forward
+    and the exact backward gives the forward bit for bit and the gradient of
+    the calls that build their own; with negative densities its sign word sends
+    the backward to the checkpointed adjoint, as the own build's does."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    ops = ngt()
+    lib = L.load()
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    x32 = (RNG.uniform(0, 1, (1, 10, 12, 14, 1)) * 0.3).astype(np.float32) - np.float32(0.1 if signed else 0.0)
+    xt = T(x32, dtype)
+    Md, Vd, Pd, Fd = (ops._floats(m, w, xt.device) for m, w in ((M, 16), (V, 16), (P, 16), (F, 6)))
+    attrs = dict(interpolation="LINEAR", boundary=bm, blending_mode="BEER_LAMBERT", keep_dims=False,
+                 separate_camera_batch=True, emission_scale=(0.6, 1.2))
+    stream = ops._stream()
+
+    def run(prepared):
+        y = torch.empty((1, 3, 8, 6, 2), device="cuda")
+        r = ops._ray_args(xt, Md, Vd, Pd, Fd, [10, 8, 6], y, attrs)
+        quad = None
+        if prepared:
+            quad = torch.empty(int(lib.ngt_raymarch_quad_bytes(ctypes.byref(r))), dtype=torch.uint8, device="cuda")
+            assert lib.ngt_raymarch_quad(ctypes.byref(r), ops._ptr(quad), stream) == L.NGT_OK
+            r.quad = ops._ptr(quad)
+        ws = torch.empty(int(lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))) + 1, dtype=torch.uint8,
+                         device="cuda")
+        r.workspace, r.workspace_bytes = ops._ptr(ws), ws.numel()
+        assert lib.ngt_raymarch_fwd(ctypes.byref(r), stream) == L.NGT_OK
+        g = L.RaymarchGradArgs()
+        g.fwd = r
+        g.fwd.workspace, g.fwd.workspace_bytes = None, 0
+        gy = torch.as_tensor(np.random.default_rng(3).standard_normal((1, 3, 8, 6, 2)).astype(np.float32),
+                             device="cuda")
+        gx = torch.empty((1, 10, 12, 14, 1), device="cuda")
+        g.output, g.output_grad, g.input_grad, g.grad_mode = ops._ptr(y), ops._ptr(gy), ops._ptr(gx), L.GRAD["exact"]
+        gws = torch.empty(int(lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g))), dtype=torch.uint8,
+                          device="cuda")
+        g.workspace, g.workspace_bytes = ops._ptr(gws), gws.numel()
+        assert lib.ngt_raymarch_bwd(ctypes.byref(g), stream) == L.NGT_OK
+        torch.cuda.synchronize()
+        flag = int(quad[:4].view(torch.int32).item()) if prepared else None
+        return y, gx, flag, ws.numel(), gws.numel()
+
+    y0, g0, _, fw0, bw0 = run(False)
+    y1, g1, flag, fw1, bw1 = run(True)
+    assert torch.equal(y0, y1)
+    assert rel(N(g0), N(g1)) < 1e-6
+    assert (flag != 0) == signed
+    assert fw1 < fw0 and bw1 < bw0  # the prepared layout is not sized again
+
+
+def test_raymarch_autograd_signed_extinction_emission():
+    """Autograd over the emission-expanded one-channel raymarch keeps the
+    forward's quad layout for the backward; with negative densities its sign
+    word selects the checkpointed adjoint (against the oracle)."""
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    rho = (RNG.uniform(0, 1, (1, 10, 12, 14, 1)) * 0.3 - 0.08).astype(np.float32)
+    scale = [0.7, 1.3]
+    full = (rho * np.asarray(scale, np.float32)).astype(np.float32)
+    rt = T(rho).requires_grad_()
+    y = ngt().raymarch_grid_transform(rt, M, V, P, F, [10, 8, 6], emission_scale=scale)
+    ref = oops.raymarch_grid_transform(full, M, V, P, F, [10, 8, 6])
+    assert rel(ref, N(y)) < 2e-5
+    gy = RNG.standard_normal(ref.shape).astype(np.float32)
+    y.backward(T(gy))
+    gfull = oops.raymarch_grid_transform_grad(full, ref, gy, M, V, P, F, [10, 8, 6], grad_mode="exact")
+    assert rel((gfull * np.asarray(scale)).sum(-1, keepdims=True), N(rt.grad)) < 1e-4
+
+
 @pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
 @pytest.mark.parametrize("dhw", [(1, 5, 6), (7, 1, 4), (5, 6, 1)])
 def test_raymarch_thin_grids(bm, dhw):
