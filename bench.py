@@ -334,7 +334,6 @@ def kernel_stats(step, torch, dev, w, st, iters, flush):
     """Average device time of each C-ABI call of the step (events around each
     call, L2 flushed before each step) and the algorithmic bytes it moves."""
     import ctypes
-    from ngt_gb300 import _lib as L
     from ngt_gb300.ops import _ptr
     es = torch.tensor([], dtype=st).element_size()
     n_rho = 128 ** 3
@@ -342,16 +341,16 @@ def kernel_stats(step, torch, dev, w, st, iters, flush):
     px = 5 * 256 * 256
     nbytes = {
         "advect_fwd": es * (2 * n_rho + n_u),                 # rho, u read; rho' written
-        "raymarch_fwd": es * n_rho + 4 * 2 * px,              # rho' read; image written
-        "image_l2_loss": 4 * (2 * px + px + 2 * px),          # image, target read; image grad written
+        "raymarch_quad": es * n_rho,                          # rho' read (its gather layout is scratch)
+        "raymarch_fwd_l2": es * n_rho + 4 * (2 * px + px + 2 * px),  # rho' read; image, target, image grad
         "raymarch_bwd": es * n_rho + 4 * (2 * px * 2) + 4 * n_rho,  # rho', image, grad read; d rho' written
         "advect_bwd": es * (n_rho + n_u) + 4 * (n_rho + n_rho) + 4 * (n_rho + n_u),  # rho,u,fwd,grad in; grads out
     }
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     calls = [("advect_fwd", lambda: step._call("ngt_advect_maccormack_fwd", ctypes.byref(step.adv), s)),
-             ("raymarch_fwd", lambda: step._call("ngt_raymarch_fwd", ctypes.byref(step.ray), s)),
-             ("image_l2_loss", lambda: step._call("ngt_image_l2_loss", L.F32 if st != torch.float64 else L.F64, step.pixels, 2, 1, _ptr(step.image),
-                                                  _ptr(step.targets), _ptr(step.g_image), _ptr(step.loss), s)),
+             ("raymarch_quad", lambda: step._call("ngt_raymarch_quad", ctypes.byref(step.ray), _ptr(step.ray_quad), s)),
+             ("raymarch_fwd_l2", lambda: step._call("ngt_raymarch_fwd_l2", ctypes.byref(step.ray), _ptr(step.targets), 1,
+                                                    _ptr(step.g_image), _ptr(step.loss), s)),
              ("raymarch_bwd", lambda: step._call("ngt_raymarch_bwd", ctypes.byref(step.ray_g), s)),
              ("advect_bwd", lambda: step._call("ngt_advect_maccormack_bwd", ctypes.byref(step.adv_g), s))]
     tot = {n: 0.0 for n, _ in calls}

@@ -406,6 +406,14 @@ int ngt_advect_maccormack_bwd_batch(const ngt_advect_grad_args* grids, int32_t c
  * with TensorFlow ops. */
 int ngt_image_l2_loss(int32_t dtype, int64_t pixels, int32_t channels, int32_t loss_channels, const void* image,
                       const void* target, void* image_grad, void* loss, void* stream);
+/* ngt_raymarch_fwd with ngt_image_l2_loss fused into its epilogue: each ray's
+ * pixel, once blended, also writes its image gradient (target: loss_channels
+ * per pixel; image_grad: the output's shape) and the loss is added to *loss per
+ * block (zero it first).  One launch instead of two; the loss differs from the
+ * separate call's only by the order of its additions.  No reference
+ * counterpart (see ngt_image_l2_loss). */
+int ngt_raymarch_fwd_l2(const ngt_raymarch_args* args, const void* target, int32_t loss_channels, void* image_grad,
+                        void* loss, void* stream);
 
 /* ------------------------------------------------------------ diagnostics */
 const char* ngt_last_error_message(void);

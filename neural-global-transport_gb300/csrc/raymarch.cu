@@ -49,6 +49,12 @@ struct RayParams {
   const void* quad;      // quad layout of the input (one channel, LINEAR) or null
   float4* gquad;         // quad gradient accumulator (exact backward) or null
   QuadDims qd;
+  // forward with the image L2 loss fused: per-pixel target (l2_lc channels),
+  // image gradient (CB channels) and the loss accumulator, or null
+  const void* l2_target;
+  void* l2_grad;
+  void* l2_loss;
+  int l2_lc;
 };
 
 // One-channel float / 16-bit grids sampled LINEAR go through the quad layout.
@@ -246,11 +252,47 @@ __device__ __forceinline__ bool tile_pixel(const RayParams& p, int tile, int& px
   return px < p.W && py < p.H;
 }
 
-// The forward of one 16x8 tile of rays of (batch b, output slot oslot).
+// Fused image L2 loss of one pixel: the gradient g_c = out_c - target_c on the
+// first l2_lc channels (0 on the others) is written, sum g_c^2 returned.
+template <int CB, class S>
+__device__ __forceinline__ S l2_pixel(const RayParams& p, int64_t pix, const S out[CB]) {
+  const S* tg = static_cast<const S*>(p.l2_target) + pix * p.l2_lc;
+  S* gr = static_cast<S*>(p.l2_grad) + pix * CB;
+  S l = S(0);
+#pragma unroll
+  for (int k = 0; k < CB; ++k) {
+    const S g = k < p.l2_lc ? out[k] - tg[k] : S(0);
+    gr[k] = g;
+    l += g * g;
+  }
+  return l;
+}
+
+// Adds 0.5 * the block's sum of ``v`` to *loss (one atomic per block); every
+// thread of the block calls it.
+template <class S>
+__device__ __forceinline__ void l2_block_add(S v, S* loss) {
+  __shared__ S part[kThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    S w = threadIdx.x < kThreads / 32 ? part[threadIdx.x] : S(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (threadIdx.x == 0) atomicAdd(loss, S(0.5) * w);
+  }
+}
+
+// The forward of one 16x8 tile of rays of (batch b, output slot oslot).  With
+// the fused loss it returns the pixel's sum of squared image differences (0
+// outside the image), else 0.
 template <int CIN, int CB, class T, class S>
-__device__ __forceinline__ void fwd_tile(const RayParams& p, const Cam& cam, int b, int oslot, int tile) {
+__device__ __forceinline__ S fwd_tile(const RayParams& p, const Cam& cam, int b, int oslot, int tile) {
   int px, py;
-  if (!tile_pixel(p, tile, px, py)) return;
+  if (!tile_pixel(p, tile, px, py)) return S(0);
+  const int64_t pix = (int64_t(oslot) * p.H + py) * p.W + px;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
   const void* qg = quad_of<CIN, T>(p, b);
   const Ray r = ray_setup(cam, px, py, p);
@@ -279,11 +321,14 @@ __device__ __forceinline__ void fwd_tile(const RayParams& p, const Cam& cam, int
 #pragma unroll
         for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
       }
-      S* out = reinterpret_cast<S*>(p.output) + ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
+      S res[CB];
 #pragma unroll
-      for (int k = 0; k < CB - 1; ++k) out[k] = L[k];
-      out[CB - 1] = dd;
-      return;
+      for (int k = 0; k < CB - 1; ++k) res[k] = L[k];
+      res[CB - 1] = dd;
+      S* out = reinterpret_cast<S*>(p.output) + pix * CB;
+#pragma unroll
+      for (int k = 0; k < CB; ++k) out[k] = res[k];
+      return p.l2_target ? l2_pixel<CB, S>(p, pix, res) : S(0);
     }
   }
   if (r.hit) {
@@ -296,9 +341,10 @@ __device__ __forceinline__ void fwd_tile(const RayParams& p, const Cam& cam, int
       for (int a = 0; a < 3; ++a) pos[a] += r.st[a];
     }
   }
-  S* out = reinterpret_cast<S*>(p.output) + ((int64_t(oslot) * p.H + py) * p.W + px) * CB;
+  S* out = reinterpret_cast<S*>(p.output) + pix * CB;
 #pragma unroll
   for (int k = 0; k < CB; ++k) out[k] = acc[k];
+  return p.l2_target ? l2_pixel<CB, S>(p, pix, acc) : S(0);
 }
 
 template <int CIN, int CB, class T, class S>
@@ -309,7 +355,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_fwd(RayParams
   slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
   load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
   __syncthreads();
-  fwd_tile<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
+  const S l = fwd_tile<CIN, CB, T, S>(p, cam, b, oslot, blockIdx.x);
+  if (p.l2_loss) l2_block_add<S>(l, static_cast<S*>(p.l2_loss));
 }
 
 // ------------------------------------------------------- exact backward
@@ -1060,16 +1107,23 @@ extern "C" size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* a) {
   return a ? fwd_layout(a).total : 0;
 }
 
-// With a workspace the cameras are formed once per call and a one-channel
-// LINEAR input is gathered through the quad layout; without one every block
-// forms its camera and gathers directly (same results).
-extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
+namespace {
+// The forward of ngt_raymarch_fwd / ngt_raymarch_fwd_l2.  With a workspace the
+// cameras are formed once per call and a one-channel LINEAR input is gathered
+// through the quad layout; without one every block forms its camera and gathers
+// directly (same results).
+int raymarch_fwd(const ngt_raymarch_args* a, const void* l2_target, int l2_lc, void* l2_grad, void* l2_loss,
+                 void* stream, const char* name) {
   int cin, cb;
   int rc = validate(a, cin, cb);
   if (rc) return rc;
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null output");
   RayParams p = make_params(a);
   if ((rc = check_prepared_quad(a))) return rc;
+  p.l2_target = l2_target;
+  p.l2_lc = l2_lc;
+  p.l2_grad = l2_grad;
+  p.l2_loss = l2_loss;
   cudaStream_t st = as_stream(stream);
   if (a->cameras) p.cams = static_cast<const Cam*>(a->cameras);
   if (a->quad) {
@@ -1092,7 +1146,22 @@ extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
   const int tiles = ceil_div_u(p.W, kTileX) * ceil_div_u(p.H, kTileY);
   rc = launch_slots(a->dtype, FWD, cin, cb, tiles, st, p);
   if (rc) return rc;
-  return check_launch("ngt_raymarch_fwd");
+  return check_launch(name);
+}
+}  // namespace
+
+extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
+  return raymarch_fwd(a, nullptr, 0, nullptr, nullptr, stream, "ngt_raymarch_fwd");
+}
+
+extern "C" int ngt_raymarch_fwd_l2(const ngt_raymarch_args* a, const void* target, int32_t loss_channels,
+                                   void* image_grad, void* loss, void* stream) {
+  if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null arguments");
+  if (!target || !image_grad || !loss) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2: null pointer");
+  const int cb = a->emission_channels ? a->emission_channels : int(a->input_shape[4]);
+  if (loss_channels <= 0 || loss_channels > cb)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2: loss_channels must be in 1..%d", cb);
+  return raymarch_fwd(a, target, loss_channels, image_grad, loss, stream, "ngt_raymarch_fwd_l2");
 }
 
 extern "C" size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* a) {

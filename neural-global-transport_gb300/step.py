@@ -25,10 +25,10 @@ from .ops import _code, _ptr
 class RenderAdvectStep:
     # kernels of one f32 exact Beer-Lambert step: advect fwd 2, the quad layout of
     # the advected density with its extinction-sign check (shared by the render's
-    # forward and backward) 1, raymarch fwd 1, loss 1, raymarch bwd 2 (the
-    # one-pass march -- checkpointed where the sign check fails -- and the fold),
-    # advect bwd 2
-    KERNELS_PER_STEP = 9
+    # forward and backward) 1, raymarch fwd with the image loss in its epilogue 1,
+    # raymarch bwd 2 (the one-pass march -- checkpointed where the sign check
+    # fails -- and the fold), advect bwd 2
+    KERNELS_PER_STEP = 8
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact"):
@@ -127,19 +127,20 @@ class RenderAdvectStep:
             raise L.NGTError(rc, self.lib.ngt_last_error_message().decode(errors="replace"))
 
     def forward(self, stream=None):
+        """Advect, render and the image loss (its gradient included), added to
+        ``self.loss``."""
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream if stream is None else stream)
         self._call("ngt_advect_maccormack_fwd", ctypes.byref(self.adv), s)
         if self.ray_quad is not None:
             self._call("ngt_raymarch_quad", ctypes.byref(self.ray), _ptr(self.ray_quad), s)
-        self._call("ngt_raymarch_fwd", ctypes.byref(self.ray), s)
+        self._call("ngt_raymarch_fwd_l2", ctypes.byref(self.ray), _ptr(self.targets), 1, _ptr(self.g_image),
+                   _ptr(self.loss), s)
 
     def launch(self):
         """Enqueue forward + loss + backward on the current stream."""
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self.loss.zero_()
         self.forward(s.value)
-        self._call("ngt_image_l2_loss", _code(self.image), self.pixels, 2, 1, _ptr(self.image), _ptr(self.targets),
-                   _ptr(self.g_image), _ptr(self.loss), s)
         self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g), s)
         self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_g), s)
 
@@ -148,8 +149,6 @@ class RenderAdvectStep:
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self.loss.zero_()
         self.forward(s.value)
-        self._call("ngt_image_l2_loss", _code(self.image), self.pixels, 2, 1, _ptr(self.image), _ptr(self.targets),
-                   _ptr(self.g_image), _ptr(self.loss), s)
         return self.loss
 
     def capture(self):

@@ -343,6 +343,51 @@ def test_raymarch_prepared_quad(dtype, bm, signed):
     assert fw1 < fw0 and bw1 < bw0  # the prepared layout is not sized again
 
 
+@pytest.mark.parametrize("case", ["quad_f32", "emission_f64", "two_channel_f32"])
+def test_raymarch_fwd_fused_l2(case):
+    """ngt_raymarch_fwd_l2 against ngt_raymarch_fwd followed by
+    ngt_image_l2_loss: the same image and image gradient bit for bit, the loss
+    up to the order of its additions."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    ops = ngt()
+    lib = L.load()
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    dt = torch.float64 if case == "emission_f64" else torch.float32
+    C = 2 if case == "two_channel_f32" else 1
+    x = T((RNG.uniform(0, 1, (1, 10, 12, 14, C)) * 0.3).astype(np.float32), dt)
+    Md, Vd, Pd, Fd = (ops._floats(m, w, x.device) for m, w in ((M, 16), (V, 16), (P, 16), (F, 6)))
+    attrs = dict(interpolation="LINEAR", boundary="BORDER", blending_mode="BEER_LAMBERT", keep_dims=False,
+                 separate_camera_batch=True, emission_scale=None if C == 2 else (0.6, 1.2))
+    tgt = torch.as_tensor(RNG.uniform(0, 0.2, (1, 3, 8, 6, 1)), device="cuda", dtype=dt)
+    stream = ops._stream()
+
+    def run(fused):
+        y = torch.empty((1, 3, 8, 6, 2), device="cuda", dtype=dt)
+        gy = torch.full_like(y, float("nan"))
+        loss = torch.zeros((1,), device="cuda", dtype=dt)
+        r = ops._ray_args(x, Md, Vd, Pd, Fd, [10, 8, 6], y, attrs)
+        ws = torch.empty(max(int(lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))), 1), dtype=torch.uint8,
+                         device="cuda")
+        r.workspace, r.workspace_bytes = ops._ptr(ws), ws.numel()
+        if fused:
+            rc = lib.ngt_raymarch_fwd_l2(ctypes.byref(r), ops._ptr(tgt), 1, ops._ptr(gy), ops._ptr(loss), stream)
+            assert rc == L.NGT_OK, lib.ngt_last_error_message()
+        else:
+            assert lib.ngt_raymarch_fwd(ctypes.byref(r), stream) == L.NGT_OK
+            assert lib.ngt_image_l2_loss(ops._code(y), 3 * 8 * 6, 2, 1, ops._ptr(y), ops._ptr(tgt), ops._ptr(gy),
+                                         ops._ptr(loss), stream) == L.NGT_OK
+        torch.cuda.synchronize()
+        return y, gy, float(loss.item())
+
+    y0, g0, l0 = run(False)
+    y1, g1, l1 = run(True)
+    assert torch.equal(y0, y1) and torch.equal(g0, g1)
+    assert abs(l1 - l0) <= 1e-6 * abs(l0) and l0 > 0
+    want = 0.5 * float(((y0[..., :1] - tgt) ** 2).sum())
+    assert abs(l1 - want) <= 1e-5 * want
+
+
 def test_raymarch_autograd_signed_extinction_emission():
     """Autograd over the emission-expanded one-channel raymarch keeps the
     forward's quad layout for the backward; with negative densities its sign
