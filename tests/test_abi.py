@@ -173,3 +173,21 @@ def test_prepared_quad_validation(lib):
         assert b"prepared quad" in lib.ngt_last_error_message()
         r.quad = None
         setattr(r, field, old)
+
+
+def test_fused_l2_forward_validation(lib):
+    from ngt_gb300 import _lib as L
+    r = L.RaymarchArgs()
+    r.dtype = L.F32
+    r.input_shape = L.I64x5(1, 4, 4, 4, 1)
+    r.output_dhw = L.I64x3(4, 4, 4)
+    for f in ("input", "output", "matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(r, f, ctypes.c_void_p(0x1000))
+    r.num_cameras = 1
+    r.interpolation, r.boundary, r.blending_mode, r.separate_camera_batch = 1, 0, 0, 1
+    r.emission_channels = 2
+    p = ctypes.c_void_p(0x2000)
+    assert lib.ngt_raymarch_fwd_l2(ctypes.byref(r), p, 3, p, p, None) == L.NGT_ERR_INVALID_ARGUMENT  # > 2 channels
+    assert lib.ngt_raymarch_fwd_l2(ctypes.byref(r), p, 0, p, p, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_raymarch_fwd_l2(ctypes.byref(r), None, 1, p, p, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_raymarch_fwd_l2(None, p, 1, p, p, None) == L.NGT_ERR_INVALID_ARGUMENT
