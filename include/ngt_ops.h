@@ -307,6 +307,13 @@ typedef struct {
    * the backward then reads it instead of re-gathering the corner extrema.
    * Null: recomputed.  No reference counterpart (TF keeps the tf.where mask). */
   void* mask;
+  /* Optional, MacCormack with MC_SMOOTH: scratch of 2 x C compute-type values
+   * per cell (float, double for F64) where forward 1 leaves the forward trace's
+   * corner extrema, taken from the same corner fetch as its trilinear value;
+   * forward 2 (and a backward without a stored mask) reads them instead of
+   * gathering the eight corners again.  Null: gathered again.  No reference
+   * counterpart. */
+  void* extrema;
 } ngt_advect_args;
 
 typedef struct {

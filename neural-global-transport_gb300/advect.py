@@ -32,7 +32,7 @@ def _faces(t, name):
     return t.contiguous()
 
 
-def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None):
+def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None, extrema=None):
     a = L.AdvectArgs()
     a.dtype = _code(data)
     D, H, W, C = data.shape
@@ -45,6 +45,7 @@ def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None):
     a.boundary = L.BOUNDARY[boundary]
     a.output, a.fwd_field = _ptr(out), _ptr(fwd)
     a.mask = _ptr(mask)
+    a.extrema = _ptr(extrema)
     return a
 
 
@@ -60,10 +61,13 @@ def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary=
     MC_SMOOTH revert mask (when ``keep_mask``) kept for the backward."""
     out = torch.empty_like(data)
     fwd = torch.empty(data.shape, dtype=compute_dtype(data), device=data.device) if order == 2 else None
-    mask = (torch.empty(data.shape, dtype=torch.uint8, device=data.device)
-            if keep_mask and order == 2 and clamp.upper() == "MC_SMOOTH" else None)
+    smooth = order == 2 and clamp.upper() == "MC_SMOOTH"
+    mask = torch.empty(data.shape, dtype=torch.uint8, device=data.device) if keep_mask and smooth else None
+    # the forward trace's corner extrema, passed from forward 1 to forward 2
+    ext = torch.empty(data.shape[:3] + (2 * data.shape[3],), dtype=compute_dtype(data),
+                      device=data.device) if smooth else None
     L.call("ngt_advect_maccormack_fwd",
-           ctypes.byref(_args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask)), _stream())
+           ctypes.byref(_args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask, ext)), _stream())
     return out, fwd, mask
 
 

@@ -73,6 +73,8 @@ class AdvectRenderChain:
 
         # MC_SMOOTH revert masks of the segment's frames (forward writes, backward reads)
         self.seg_mask = torch.empty((K, D, H, W, 1), dtype=torch.uint8, device=dev)
+        # forward 1 -> forward 2 corner extrema of every advection (stream-ordered, one buffer)
+        self.adv_ext = torch.empty((D, H, W, 2), dtype=cd, device=dev)
 
         def advect_args(data, out, fwd, mask=None):
             a = L.AdvectArgs()
@@ -83,6 +85,7 @@ class AdvectRenderChain:
             a.dt, a.order, a.clamp, a.boundary = float(dt), 2, L.CLAMP[clamp], L.BOUNDARY[advect_boundary]
             a.output, a.fwd_field = _ptr(out), _ptr(fwd)
             a.mask = _ptr(mask)
+            a.extrema = _ptr(self.adv_ext)
             return a
 
         # chain forward: cur[t % 2] -> cur[(t + 1) % 2]

@@ -117,6 +117,8 @@ struct McParams {
   CT<T>* gback;        // deterministic mode: back-trace gradient per cell (gathered afterwards)
   CT<T>* gface[3];     // density, non-deterministic: face gradients accumulated by backward 2
   uint8_t* mask;       // MC_SMOOTH revert mask: written by forward 2, read by backward 1 (optional)
+  CT<T>* ext;          // MC_SMOOTH: the forward trace's corner extrema (min, max per cell and channel),
+                       //   written by forward 1, read instead of gathered again (optional)
   float dt;            // with gface: the lookup is centred(u) * (-dt)
   Dims d;
   int order, clamp, bm, reference;
@@ -137,6 +139,38 @@ __device__ __forceinline__ void mc_fwd1_at(const McParams<T>& p, const LK& lk, i
   S lut[3];
   lk(x, y, z, lut);
   S v[C];
+  if (p.ext && p.order == 2 && p.clamp == NGT_CLAMP_MC_SMOOTH) {
+    // the trilinear value and the corner extrema from one fetch of the eight
+    // corners (read_linear and read_minmax: out-of-range BORDER corners read 0,
+    // which is also what read_minmax's extrema start from when one is out)
+    const Tri<S> t = tri_setup(add_rn(lut[0], S(x)), add_rn(lut[1], S(y)), add_rn(lut[2], S(z)), p.d, p.bm);
+    S mn[C], mx[C];
+    if (p.bm == BORDER && !t.inside) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) v[c] = mn[c] = mx[c] = S(0);
+    } else {
+      S vc[8][C];
+      tri_fetch<C>(p.data, t, p.d, vc);
+      tri_combine<C>(vc, t, v);
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        mn[c] = S(kFloatMax);
+        mx[c] = S(-kFloatMax);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          if (vc[k][c] < mn[c]) mn[c] = vc[k][c];
+          if (vc[k][c] > mx[c]) mx[c] = vc[k][c];
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      p.fwd[i * C + c] = v[c];
+      p.ext[(i * C + c) * 2 + 0] = mn[c];
+      p.ext[(i * C + c) * 2 + 1] = mx[c];
+    }
+    return;
+  }
   read_linear<C>(p.data, add_rn(lut[0], S(x)), add_rn(lut[1], S(y)), add_rn(lut[2], S(z)), p.d, p.bm, v);
   if (p.order == 1) {
 #pragma unroll
@@ -183,7 +217,13 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
   }
   S mn[C], mx[C];
   const bool recompute = p.clamp == NGT_CLAMP_MC_SMOOTH && !(stored && p.mask);
-  if (recompute) {
+  if (recompute && p.ext) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      mn[c] = p.ext[(i * C + c) * 2 + 0];
+      mx[c] = p.ext[(i * C + c) * 2 + 1];
+    }
+  } else if (recompute) {
     const S p1x = add_rn(lut[0], S(x)), p1y = add_rn(lut[1], S(y)), p1z = add_rn(lut[2], S(z));
     read_minmax<C>(p.data, p1x, p1y, p1z, p.d, p.bm, mn, mx);
   }
@@ -632,6 +672,7 @@ McParams<T> density_params(const ngt_advect_args* a) {
   p.out = static_cast<T*>(a->output);
   p.fwd = static_cast<CT<T>*>(a->fwd_field);
   p.mask = static_cast<uint8_t*>(a->mask);
+  p.ext = static_cast<CT<T>*>(a->extrema);
   p.d = cells_of(a->grid_dhw);
   p.order = a->order;
   p.clamp = a->clamp;

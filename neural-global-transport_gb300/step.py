@@ -71,6 +71,9 @@ class RenderAdvectStep:
         # the forward's MC_SMOOTH revert mask, read back by the backward
         self.mc_mask = torch.empty((D, H, W, 1), dtype=torch.uint8, device=dev)
         a.mask = _ptr(self.mc_mask)
+        # forward 1 hands the forward trace's corner extrema to forward 2
+        self.mc_ext = torch.empty((D, H, W, 2), dtype=f32, device=dev)
+        a.extrema = _ptr(self.mc_ext)
         self.adv = a
         ag = L.AdvectGradArgs()
         ag.fwd = a

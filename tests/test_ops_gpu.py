@@ -586,6 +586,34 @@ def test_advect_backward_deterministic(bm):
 
 
 @pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
+@pytest.mark.parametrize("C", [1, 2, 4])
+def test_advect_stored_extrema_bitexact(bm, C):
+    """MacCormack forward with the corner extrema handed from forward 1 to
+    forward 2 against the forward gathering them again: identical outputs,
+    masks and forward fields."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    from ngt_gb300 import advect
+    ops = ngt()
+    rho, ux, uy, uz = advect_inputs(shape=(9, 12, 14), seed=37)
+    rho = np.concatenate([rho * (k + 1) for k in range(C)], -1) - np.float32(0.05)
+    ts = [T(a) for a in (rho, ux, uy, uz)]
+    res = []
+    for with_ext in (False, True):
+        out = torch.empty_like(ts[0])
+        fwd = torch.empty_like(ts[0])
+        mask = torch.empty(ts[0].shape, dtype=torch.uint8, device="cuda")
+        ext = torch.empty(ts[0].shape[:3] + (2 * C,), device="cuda") if with_ext else None
+        a = advect._args(*ts, out, fwd, 1.0, 2, "MC_SMOOTH", bm, mask, ext)
+        assert L.load().ngt_advect_maccormack_fwd(ctypes.byref(a), ops._stream()) == L.NGT_OK
+        torch.cuda.synchronize()
+        res.append((out, fwd, mask))
+    for a, b in zip(*res):
+        assert torch.equal(a, b)
+    assert int(res[0][2].sum()) > 0
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
 def test_advect_stored_mask_matches_recomputed(bm):
     """The backward reading the forward's stored MC_SMOOTH mask equals the
     backward recomputing it from the corner extrema."""
