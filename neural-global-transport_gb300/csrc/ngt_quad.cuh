@@ -100,14 +100,59 @@ __device__ __forceinline__ void quad_build_at(const T* __restrict__ g, const Dim
   q[int64_t(b) * qd.count + e] = o;
 }
 
+// Planes of entries one thread of k_quad_build fills (the (x, y) boundary
+// mapping and the sign vote are then shared by those planes).
+constexpr int kQuadPlanes = 4;
+
+// One thread per (xq, yq) and kQuadPlanes consecutive planes of the N * (D + 2)
+// planes (blockIdx.z = first plane / kQuadPlanes); quad_build_at's entries.
 template <class T>
 __global__ void k_quad_build(const T* __restrict__ g, Dims d, int bm, typename QuadOf<T>::type* __restrict__ q,
-                             int* neg, float scale) {
+                             int* neg, float scale, int planes) {
   const QuadDims qd = QuadDims::of(d);
   const int xq = int(blockIdx.x * blockDim.x + threadIdx.x), yq = int(blockIdx.y * blockDim.y + threadIdx.y);
-  if (xq >= qd.x || yq >= qd.y) return;
-  const int b = int(blockIdx.z) / qd.z, zq = int(blockIdx.z) - b * qd.z;
-  quad_build_at<T>(g, d, bm, q, neg, scale, xq, yq, zq, b);
+  const bool in = xq < qd.x && yq < qd.y;
+  bool vx0 = false, vx1 = false, vy0 = false, vy1 = false;
+  int x0 = 0, x1 = 0, y0 = 0, y1 = 0;
+  if (in) {
+    x0 = quad_cell(xq - 1, d.x, bm, vx0);
+    x1 = quad_cell(xq, d.x, bm, vx1);
+    y0 = quad_cell(yq - 1, d.y, bm, vy0);
+    y1 = quad_cell(yq, d.y, bm, vy1);
+  }
+  const int64_t plane_cells = int64_t(d.x) * d.y;
+  const T zero = T(0.0f);
+  bool n = false;
+  const int first = int(blockIdx.z) * kQuadPlanes;
+#pragma unroll
+  for (int k = 0; k < kQuadPlanes; ++k) {
+    const int zz = first + k;
+    if (!in || zz >= planes) break;
+    const int b = zz / qd.z, zq = zz - b * qd.z;
+    bool vz;
+    const int z = quad_cell(zq - 1, d.z, bm, vz);
+    const T* pl = g + (int64_t(b) * d.z + z) * plane_cells;
+    const T* r0 = pl + int64_t(y0) * d.x;
+    const T* r1 = pl + int64_t(y1) * d.x;
+    T v[4];
+    v[0] = (vz && vy0 && vx0) ? r0[x0] : zero;
+    v[1] = (vz && vy0 && vx1) ? r0[x1] : zero;
+    v[2] = (vz && vy1 && vx0) ? r1[x0] : zero;
+    v[3] = (vz && vy1 && vx1) ? r1[x1] : zero;
+    if (neg) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) n = n || (scale * float(v[c]) < 0.0f);
+    }
+    typename QuadOf<T>::type o;
+    if constexpr (sizeof(T) == 4) {
+      o = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+      o.x = raw16(v[0]) | (raw16(v[1]) << 16);
+      o.y = raw16(v[2]) | (raw16(v[3]) << 16);
+    }
+    q[int64_t(b) * qd.count + (int64_t(zq) * qd.y + yq) * qd.x + xq] = o;
+  }
+  if (neg && __any_sync(0xffffffffu, n) && n) atomicOr(neg, 1);
 }
 
 template <class T>

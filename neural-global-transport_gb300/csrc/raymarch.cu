@@ -1022,20 +1022,21 @@ int build_quad(const ngt_raymarch_args* a, void* q, cudaStream_t st, int* neg = 
   const Dims d = in_dims(a);
   const QuadDims qd = QuadDims::of(d);
   CellLaunch l = cell_launch(Dims{qd.x, qd.y, qd.z});
-  l.grid.z = unsigned(qd.z * a->input_shape[0]);
+  const int planes = int(qd.z * a->input_shape[0]);
+  l.grid.z = unsigned((planes + kQuadPlanes - 1) / kQuadPlanes);
   const dim3 grid = l.grid, blk = l.block;
   switch (a->dtype) {
     case NGT_F32:
       k_quad_build<float><<<grid, blk, 0, st>>>(static_cast<const float*>(a->input), d, a->boundary,
-                                                 static_cast<float4*>(q), neg, scale);
+                                                 static_cast<float4*>(q), neg, scale, planes);
       break;
     case NGT_BF16:
       k_quad_build<__nv_bfloat16><<<grid, blk, 0, st>>>(static_cast<const __nv_bfloat16*>(a->input), d,
-                                                         a->boundary, static_cast<uint2*>(q), neg, scale);
+                                                         a->boundary, static_cast<uint2*>(q), neg, scale, planes);
       break;
     case NGT_F16:
       k_quad_build<__half><<<grid, blk, 0, st>>>(static_cast<const __half*>(a->input), d, a->boundary,
-                                                  static_cast<uint2*>(q), neg, scale);
+                                                  static_cast<uint2*>(q), neg, scale, planes);
       break;
     default:
       return fail(NGT_ERR_UNSUPPORTED, "raymarch: quad layout needs float or 16-bit storage");
