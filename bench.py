@@ -132,7 +132,7 @@ class ClockSampler:
 # DRAM bytes (read + write) per call of the dominant library call, summed over its
 # kernels, from one ncu capture of this workload in f32 (cold cache per kernel):
 # profiles/step_f32_128cube_5views_kernels.md
-NCU_TRAFFIC_F32 = {"raymarch_bwd": 116.43e6}
+NCU_TRAFFIC_F32 = {"raymarch_bwd": 107.90e6}
 
 
 def measured_peak_hbm():
