@@ -12,6 +12,7 @@ or ``"reference"`` (the reference's count / weight normalised gradients).
 
 All tensors must be contiguous CUDA tensors; there is no CPU path.
 """
+import collections
 import contextlib
 import ctypes
 
@@ -89,19 +90,75 @@ def _enum(table, value, name):
     return table[v]
 
 
+# Device copies of host matrices, by content, and camera blocks formed from them
+# (cameras are usually the same from one call to the next).  Entries are made on
+# the caller's stream; a call on another stream waits for that stream's event.
+_CACHE_SIZE = 32
+_HOST_MATS = collections.OrderedDict()  # (shape, bytes, width, device) -> (tensor, event, stream)
+_CAMERAS = collections.OrderedDict()    # (ids of cached matrices, slots) -> (block, event, stream, matrices)
+
+
+def _cache_put(cache, key, value):
+    cache[key] = value
+    if len(cache) > _CACHE_SIZE:
+        cache.popitem(last=False)
+
+
+def _cache_get(cache, key):
+    hit = cache.get(key)
+    if hit is None:
+        return None
+    cache.move_to_end(key)
+    stream = torch.cuda.current_stream(hit[0].device)
+    if stream.cuda_stream != hit[2]:
+        stream.wait_event(hit[1])
+    return hit[0]
+
+
+def _recorded(t):
+    ev = torch.cuda.Event()
+    stream = torch.cuda.current_stream(t.device)
+    ev.record(stream)
+    return ev, stream.cuda_stream
+
+
 def _floats(m, width, device):
     """Matrices / frusta as the contiguous float32 device buffer the kernels read:
     the C-order flattening of what the caller passed, ``width`` floats per entry.
 
-    Host arrays go through pinned staging memory with a stream-ordered copy: a copy
-    from pageable memory would first wait for all work queued on the stream, so
-    every call taking numpy matrices would stall the host behind the GPU."""
+    Host arrays are uploaded once per content and device (through pinned memory
+    with a stream-ordered copy: a copy from pageable memory would first wait for
+    all work queued on the stream) and the device copy is reused."""
+    device = torch.device(device)
+    if device.type == "cuda" and device.index is None:
+        device = torch.device("cuda", torch.cuda.current_device())
     if isinstance(m, torch.Tensor):
-        t = m.detach().to(device=device, dtype=torch.float32, non_blocking=True)
-    else:
-        host = torch.from_numpy(np.ascontiguousarray(m, dtype=np.float32))
-        t = host.pin_memory().to(device=device, non_blocking=True)
-    return t.reshape(-1, width).contiguous()
+        return m.detach().to(device=device, dtype=torch.float32, non_blocking=True).reshape(-1, width).contiguous()
+    a = np.ascontiguousarray(m, dtype=np.float32)
+    key = (a.shape, a.tobytes(), width, device.type, device.index)
+    t = _cache_get(_HOST_MATS, key)
+    if t is None:
+        t = torch.tensor(a).pin_memory().to(device=device, non_blocking=True).reshape(-1, width).contiguous()
+        t._ngt_host_key = key
+        _cache_put(_HOST_MATS, key, (t,) + _recorded(t))
+    return t
+
+
+def _cameras(r, M, V, P, F):
+    """The camera block of raymarch args ``r`` (ngt_raymarch_cameras) when all four
+    matrix buffers are cached host uploads, formed once per matrices and slot
+    layout; None otherwise (the call then forms its cameras itself)."""
+    if any(getattr(t, "_ngt_host_key", None) is None for t in (M, V, P, F)):
+        return None
+    key = (id(M), id(V), id(P), id(F), int(r.input_shape[0]), int(r.separate_camera_batch))
+    cams = _cache_get(_CAMERAS, key)
+    if cams is None:
+        lib = L.load()
+        cams = torch.empty(int(lib.ngt_raymarch_cameras_bytes(ctypes.byref(r))), dtype=torch.uint8, device=M.device)
+        L.call("ngt_raymarch_cameras", ctypes.byref(r), _ptr(cams), _stream())
+        # the entry holds the matrices, so their ids stay theirs while it lives
+        _cache_put(_CAMERAS, key, (cams,) + _recorded(cams) + ((M, V, P, F),))
+    return cams
 
 
 def _workspace(nbytes, device):
@@ -367,6 +424,9 @@ def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
     ``quad`` is None."""
     out = torch.empty(_ray_out_shape(input, V, out_dhw, a), dtype=compute_dtype(input), device=input.device)
     r = _ray_args(input, M, V, P, F, out_dhw, out, a)
+    cams = _cameras(r, M, V, P, F)
+    if cams is not None:
+        r.cameras = _ptr(cams)
     lib = L.load()
     quad = None
     if keep_quad:
@@ -384,6 +444,9 @@ def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
 def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode, quad=None):
     g = L.RaymarchGradArgs()
     g.fwd = _ray_args(input, M, V, P, F, out_dhw, None, a)
+    cams = _cameras(g.fwd, M, V, P, F)
+    if cams is not None:
+        g.fwd.cameras = _ptr(cams)
     if quad is not None and mode == "exact":
         g.fwd.quad = _ptr(quad)
     gi = torch.empty(input.shape, dtype=compute_dtype(input), device=input.device)
