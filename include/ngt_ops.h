@@ -62,7 +62,8 @@ enum { NGT_TRANSFORM_LINDEPTH = 0, NGT_TRANSFORM_LINDEPTH_REVERSE = 1, NGT_TRANS
        NGT_TRANSFORM_REVERSE = 4 };
 /* gradient semantics */
 enum { NGT_GRAD_EXACT = 0, NGT_GRAD_REFERENCE = 1 };
-/* advection clamp (data_structures.py:1715-1735) */
+/* advection clamp (data_structures.py:1715-1735); MC_SMOOTH, MacCormack's
+ * limiter, has no effect with order 1 */
 enum { NGT_CLAMP_NONE = 0, NGT_CLAMP_MC_SMOOTH = 1, NGT_CLAMP_NEGATIVE = 2 };
 
 /* ------------------------------------------------------------ LUT resample */

@@ -616,7 +616,8 @@ int validate_common(int dtype, const int64_t* dhw, int order, int clamp, int bou
   if (dhw[0] + 1 > 65535) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: depth above 65534 cells");
   if (order != 1 && order != 2) return fail(NGT_ERR_INVALID_ARGUMENT, "Unsupported warp order '%d'", order);
   if (clamp < NGT_CLAMP_NONE || clamp > NGT_CLAMP_NEGATIVE) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid clamp");
-  if (clamp == NGT_CLAMP_MC_SMOOTH && order != 2) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: MC_SMOOTH needs order 2");
+  // MC_SMOOTH is MacCormack's limiter: with order 1 it has no effect, as in
+  // VelocityGrid.warp (data_structures.py:1709-1734)
   if (boundary < NGT_BORDER || boundary > NGT_WRAP) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid boundary");
   if (dtype < NGT_F32 || dtype > NGT_F16) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: invalid dtype");
   return NGT_OK;

@@ -406,6 +406,37 @@ def test_raymarch_autograd_signed_extinction_emission():
     assert rel((gfull * np.asarray(scale)).sum(-1, keepdims=True), N(rt.grad)) < 1e-4
 
 
+def test_host_matrix_and_camera_caches():
+    """Host matrices are uploaded once per content (a changed array uploads
+    again), cameras formed from cached uploads are reused, and results equal
+    the call given device matrices (cameras formed per call)."""
+    ops = ngt()
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    dev = torch.device("cuda", 0)
+    a = ops._floats(M, 16, dev)
+    assert ops._floats(M.copy(), 16, dev) is a
+    M2 = M.copy()
+    M2[0, 12] += 0.25
+    b = ops._floats(M2, 16, dev)
+    assert b is not a and not torch.equal(a, b)
+    x = T((RNG.uniform(0, 1, (1, 10, 12, 14, 1)) * 0.3).astype(np.float32)).requires_grad_()
+    y1 = ops.raymarch_grid_transform(x, M, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
+    n_cams = len(ops._CAMERAS)
+    y2 = ops.raymarch_grid_transform(x, M, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
+    assert len(ops._CAMERAS) == n_cams and torch.equal(y1, y2)
+    y3 = ops.raymarch_grid_transform(x, torch.as_tensor(M, device=dev), torch.as_tensor(V, device=dev),
+                                     torch.as_tensor(P, device=dev), torch.as_tensor(F, device=dev), [10, 8, 6],
+                                     emission_scale=(0.5, 1.0))
+    assert torch.equal(y1, y3)
+    g = T(RNG.standard_normal(tuple(y1.shape)).astype(np.float32))
+    ga, = torch.autograd.grad(y1, x, g)
+    gb, = torch.autograd.grad(y3, x, g)
+    assert rel(N(gb), N(ga)) < 1e-6
+    # moved to the new matrix content: a different image
+    y4 = ops.raymarch_grid_transform(x, M2, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
+    assert not torch.equal(y1, y4)
+
+
 @pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
 @pytest.mark.parametrize("dhw", [(1, 5, 6), (7, 1, 4), (5, 6, 1)])
 def test_raymarch_thin_grids(bm, dhw):
