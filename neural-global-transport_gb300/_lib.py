@@ -172,9 +172,22 @@ def load():
     return _lib
 
 
+# NVTX ranges around every library call, for timelines taken with a profiler
+# (NGT_NVTX=1 in the environment; off by default, one flag test per call then).
+NVTX = os.environ.get("NGT_NVTX", "0") not in ("", "0")
+
+
 def call(name, *args):
     lib = load()
-    rc = getattr(lib, name)(*args)
+    if NVTX:
+        import torch
+        torch.cuda.nvtx.range_push(name)
+        try:
+            rc = getattr(lib, name)(*args)
+        finally:
+            torch.cuda.nvtx.range_pop()
+    else:
+        rc = getattr(lib, name)(*args)
     if rc != NGT_OK:
         raise NGTError(rc, lib.ngt_last_error_message().decode(errors="replace"))
     return rc

@@ -124,9 +124,7 @@ class BatchedScenes:
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
     def _call(self, name, *args):
-        rc = getattr(self.lib, name)(*args)
-        if rc != L.NGT_OK:
-            raise L.NGTError(rc, self.lib.ngt_last_error_message().decode(errors="replace"))
+        L.call(name, *args)
 
     # ---------------------------------------------------------------- passes
     def advect_fwd(self, s):

@@ -152,9 +152,7 @@ class AdvectRenderChain:
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
     def _call(self, name, *args):
-        rc = getattr(self.lib, name)(*args)
-        if rc != L.NGT_OK:
-            raise L.NGTError(rc, self.lib.ngt_last_error_message().decode(errors="replace"))
+        L.call(name, *args)
 
     def _l2(self, t, s):
         self._call("ngt_image_l2_loss", _code(self.image), self.pixels, 2, 1, _ptr(self.image),

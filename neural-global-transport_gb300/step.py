@@ -125,9 +125,7 @@ class RenderAdvectStep:
         self.graph = None
 
     def _call(self, name, *args):
-        rc = getattr(self.lib, name)(*args)
-        if rc != L.NGT_OK:
-            raise L.NGTError(rc, self.lib.ngt_last_error_message().decode(errors="replace"))
+        L.call(name, *args)
 
     def forward(self, stream=None):
         """Advect, render and the image loss (its gradient included), added to

@@ -191,3 +191,19 @@ def test_fused_l2_forward_validation(lib):
     assert lib.ngt_raymarch_fwd_l2(ctypes.byref(r), p, 0, p, p, None) == L.NGT_ERR_INVALID_ARGUMENT
     assert lib.ngt_raymarch_fwd_l2(ctypes.byref(r), None, 1, p, p, None) == L.NGT_ERR_INVALID_ARGUMENT
     assert lib.ngt_raymarch_fwd_l2(None, p, 1, p, p, None) == L.NGT_ERR_INVALID_ARGUMENT
+
+
+def test_nvtx_ranges_wrap_calls(monkeypatch, lib):
+    """With NVTX on, every library call sits inside one pushed / popped range,
+    also when the call fails."""
+    import torch
+    from ngt_gb300 import _lib as L
+    events = []
+    monkeypatch.setattr(L, "NVTX", True)
+    monkeypatch.setattr(torch.cuda.nvtx, "range_push", lambda n: events.append(("push", n)))
+    monkeypatch.setattr(torch.cuda.nvtx, "range_pop", lambda: events.append(("pop",)))
+    with pytest.raises(L.NGTError):
+        L.call("ngt_raymarch_fwd", None, None)
+    with pytest.raises(L.NGTError):
+        L.call("ngt_advect_maccormack_fwd", None, None)
+    assert events == [("push", "ngt_raymarch_fwd"), ("pop",), ("push", "ngt_advect_maccormack_fwd"), ("pop",)]
