@@ -125,6 +125,13 @@ class AdvectRenderChain:
             return r
 
         self.ray = [ray_args(self.seg[j + 1]) for j in range(K)]
+        # each frame's density in the quad gather layout, prepared once for the
+        # frame's render forward and backward (one buffer, frames run in order)
+        nq = int(self.lib.ngt_raymarch_quad_bytes(ctypes.byref(self.ray[0])))
+        self.ray_quad = torch.empty(nq, dtype=torch.uint8, device=dev) if nq else None
+        if nq:
+            for r in self.ray:
+                r.quad = _ptr(self.ray_quad)
         fws = max(int(self.lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))) for r in self.ray)
         self.ray_fws = torch.empty(fws, dtype=torch.uint8, device=dev)
         self.cameras = torch.empty(int(self.lib.ngt_raymarch_cameras_bytes(ctypes.byref(self.ray[0]))),
@@ -154,9 +161,12 @@ class AdvectRenderChain:
     def _call(self, name, *args):
         L.call(name, *args)
 
-    def _l2(self, t, s):
-        self._call("ngt_image_l2_loss", _code(self.image), self.pixels, 2, 1, _ptr(self.image),
-                   _ptr(self.targets[t]), _ptr(self.g_image), _ptr(self.loss), s)
+    def _render_loss(self, j, t, s):
+        """Frame t's render (segment slot j) with its image loss and gradient."""
+        if self.ray_quad is not None:
+            self._call("ngt_raymarch_quad", ctypes.byref(self.ray[j]), _ptr(self.ray_quad), s)
+        self._call("ngt_raymarch_fwd_l2", ctypes.byref(self.ray[j]), _ptr(self.targets[t]), 1, _ptr(self.g_image),
+                   _ptr(self.loss), s)
 
     # ------------------------------------------------------------------ the chain
     def launch(self):
@@ -188,8 +198,7 @@ class AdvectRenderChain:
                 self.seg[j + 1].add_(self.source)
             for j in range(s1 - s0 - 1, -1, -1):
                 t = s0 + j
-                self._call("ngt_raymarch_fwd", ctypes.byref(self.ray[j]), s)
-                self._l2(t, s)
+                self._render_loss(j, t, s)
                 self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g[j]), s)
                 self.g_rho[k].add_(self.g_render)
                 self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_bwd[(j, k)]), s)
