@@ -226,6 +226,10 @@ typedef struct {
                                  from ngt_raymarch_bwd_workspace_bytes; 256 bytes
                                  select direct gathers and scatters) */
   size_t workspace_bytes;
+  /* Exact mode: nonzero adds the input gradient to input_grad instead of
+   * writing it (a gradient summed over several renders of one grid, e.g. the
+   * frames of a chain).  The reference's ops write their outputs. */
+  int32_t accumulate;
 } ngt_raymarch_grad_args;
 
 size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* args);
@@ -328,6 +332,9 @@ typedef struct {
   int32_t deterministic;      /* exact mode: gather form, bit-reproducible gradients */
   void* workspace;
   size_t workspace_bytes;
+  /* Exact, non-deterministic mode: nonzero adds the data and velocity
+   * gradients to data_grad and vel_*_grad instead of writing them. */
+  int32_t accumulate;
 } ngt_advect_grad_args;
 
 int ngt_advect_maccormack_fwd(const ngt_advect_args* args, void* stream);

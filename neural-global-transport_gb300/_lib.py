@@ -68,7 +68,7 @@ class RaymarchArgs(ctypes.Structure):
 
 class RaymarchGradArgs(ctypes.Structure):
     _fields_ = [("fwd", RaymarchArgs), ("output", c_vp), ("output_grad", c_vp), ("input_grad", c_vp),
-                ("grad_mode", c_i32), ("workspace", c_vp), ("workspace_bytes", c_sz)]
+                ("grad_mode", c_i32), ("workspace", c_vp), ("workspace_bytes", c_sz), ("accumulate", c_i32)]
 
 
 class ReduceBlendArgs(ctypes.Structure):
@@ -90,7 +90,7 @@ class AdvectArgs(ctypes.Structure):
 class AdvectGradArgs(ctypes.Structure):
     _fields_ = [("fwd", AdvectArgs), ("output_grad", c_vp), ("data_grad", c_vp), ("vel_x_grad", c_vp),
                 ("vel_y_grad", c_vp), ("vel_z_grad", c_vp), ("grad_mode", c_i32), ("deterministic", c_i32),
-                ("workspace", c_vp), ("workspace_bytes", c_sz)]
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("accumulate", c_i32)]
 
 
 class AdvectVelocityArgs(ctypes.Structure):

@@ -67,9 +67,7 @@ class AdvectRenderChain:
         # gradients: w.r.t. the current frame's density (ping-pong), the render's part,
         # the velocity (total and one frame's)
         self.g_rho = torch.empty((2, D, H, W, 1), dtype=cd, device=dev)
-        self.g_render = torch.empty((D, H, W, 1), dtype=cd, device=dev)
         self.g_u = [torch.empty(u.shape, dtype=cd, device=dev) for u in (ux, uy, uz)]
-        self.g_u_frame = [torch.empty(u.shape, dtype=cd, device=dev) for u in (ux, uy, uz)]
 
         # MC_SMOOTH revert masks of the segment's frames (forward writes, backward reads)
         self.seg_mask = torch.empty((K, D, H, W, 1), dtype=torch.uint8, device=dev)
@@ -101,7 +99,9 @@ class AdvectRenderChain:
                 g = L.AdvectGradArgs()
                 g.fwd = self.adv_seg[j]
                 g.output_grad, g.data_grad = _ptr(self.g_rho[k]), _ptr(self.g_rho[1 - k])
-                g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (_ptr(t) for t in self.g_u_frame)
+                # the frame's velocity gradient is added to the chain's
+                g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (_ptr(t) for t in self.g_u)
+                g.accumulate = 1
                 g.grad_mode = L.GRAD["exact"]
                 ws_bytes = max(ws_bytes, int(self.lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g))))
                 self.adv_bwd[(j, k)] = g
@@ -137,19 +137,23 @@ class AdvectRenderChain:
         self.cameras = torch.empty(int(self.lib.ngt_raymarch_cameras_bytes(ctypes.byref(self.ray[0]))),
                                    dtype=torch.uint8, device=dev)
         self._call("ngt_raymarch_cameras", ctypes.byref(self.ray[0]), _ptr(self.cameras), self._stream())
-        self.ray_g = []
+        # render backward of segment slot j, its density gradient added to g_rho[k]
+        self.ray_g = {}
         bws = 0
         for r in self.ray:
             r.workspace, r.workspace_bytes = _ptr(self.ray_fws), fws
             r.cameras = _ptr(self.cameras)
-            g = L.RaymarchGradArgs()
-            g.fwd = r
-            g.output, g.output_grad, g.input_grad = _ptr(self.image), _ptr(self.g_image), _ptr(self.g_render)
-            g.grad_mode = L.GRAD["exact"]
-            bws = max(bws, int(self.lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g))))
-            self.ray_g.append(g)
+        for j, r in enumerate(self.ray):
+            for k in range(2):
+                g = L.RaymarchGradArgs()
+                g.fwd = r
+                g.output, g.output_grad, g.input_grad = _ptr(self.image), _ptr(self.g_image), _ptr(self.g_rho[k])
+                g.grad_mode = L.GRAD["exact"]
+                g.accumulate = 1
+                bws = max(bws, int(self.lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g))))
+                self.ray_g[(j, k)] = g
         self.ray_bws = torch.empty(bws, dtype=torch.uint8, device=dev)
-        for g in self.ray_g:
+        for g in self.ray_g.values():
             g.workspace, g.workspace_bytes = _ptr(self.ray_bws), bws
         self.graph = None
 
@@ -199,11 +203,9 @@ class AdvectRenderChain:
             for j in range(s1 - s0 - 1, -1, -1):
                 t = s0 + j
                 self._render_loss(j, t, s)
-                self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g[j]), s)
-                self.g_rho[k].add_(self.g_render)
-                self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_bwd[(j, k)]), s)
-                for a, b in zip(self.g_u, self.g_u_frame):
-                    a.add_(b)
+                self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g[(j, k)]), s)  # g_rho[k] += render grad
+                self.g_rho[1 - k].zero_()
+                self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_bwd[(j, k)]), s)  # and g_u +=
                 k = 1 - k
         self.result = k  # g_rho[k] = d loss / d rho_0
 

@@ -279,7 +279,7 @@ template <int C, class T, class LK>
 __device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, int x, int y, int z, bool active) {
   typedef CT<T> S;
   const int64_t i = flat(x, y, z, p.d);
-  if (p.gface[0] && active) {
+  if (p.gface[0] && active && !p.accumulate) {
     // clear the face gradients that backward 2 accumulates: each cell its lower
     // face per axis, the last cell of a line also the upper one
     S* fx = p.gface[0] + (int64_t(z) * p.d.y + y) * (p.d.x + 1) + x;
@@ -702,6 +702,7 @@ int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
   p.gdata = static_cast<S*>(g->data_grad);
   p.reference = g->grad_mode == NGT_GRAD_REFERENCE;
   p.det = !p.reference && g->deterministic;
+  p.accumulate = g->accumulate ? 1 : 0;
   char* w = static_cast<char*>(g->workspace);
   p.gfwd = reinterpret_cast<S*>(w);
   w += size_t(n) * C * sizeof(S);
@@ -1017,6 +1018,8 @@ extern "C" int ngt_advect_maccormack_bwd(const ngt_advect_grad_args* g, void* st
   if (!g->output_grad || !g->data_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "advect_bwd: null pointer");
   if (g->grad_mode != NGT_GRAD_EXACT && g->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "advect_bwd: invalid grad_mode");
+  if (g->accumulate && (g->grad_mode != NGT_GRAD_EXACT || g->deterministic))
+    return fail(NGT_ERR_UNSUPPORTED, "advect_bwd: accumulate needs the exact, non-deterministic gradient");
   const size_t need = ngt_advect_maccormack_bwd_workspace_bytes(g);
   if (!g->workspace || g->workspace_bytes < need)
     return fail(NGT_ERR_WORKSPACE, "advect_bwd needs %zu workspace bytes", need);
@@ -1101,8 +1104,8 @@ extern "C" int ngt_advect_maccormack_bwd_batch(const ngt_advect_grad_args* items
     a[i] = &g.fwd;
     if (!g.output_grad || !g.data_grad || !g.vel_x_grad || !g.vel_y_grad || !g.vel_z_grad)
       return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch backward: null pointer");
-    if (g.grad_mode != NGT_GRAD_EXACT || g.deterministic)
-      return fail(NGT_ERR_UNSUPPORTED, "advect batch backward: exact, non-deterministic gradients only");
+    if (g.grad_mode != NGT_GRAD_EXACT || g.deterministic || g.accumulate)
+      return fail(NGT_ERR_UNSUPPORTED, "advect batch backward: exact, non-deterministic, written gradients only");
   }
   int zsum, mw, mh;
   const int rc = validate_batch(a, count, zsum, mw, mh);

@@ -301,7 +301,8 @@ __device__ __forceinline__ int quad_sources(int i, int n, int bm, int src[3]) {
 // (blockIdx.z = z + D * b).  Component (kx, ky) of entry (xq, yq) is coordinate
 // (xq - 1 + kx, yq - 1 + ky) of plane zq - 1.
 __device__ __forceinline__ void quad_fold_at(const float4* __restrict__ gq, const Dims& d, int bm,
-                                             float* __restrict__ grad, int x, int y, int z, int b) {
+                                             float* __restrict__ grad, int x, int y, int z, int b,
+                                             bool accumulate = false) {
   const QuadDims qd = QuadDims::of(d);
   const int64_t i = (int64_t(z) * d.y + y) * d.x + x;
   const float4* q = gq + int64_t(b) * qd.count;
@@ -323,14 +324,16 @@ __device__ __forceinline__ void quad_fold_at(const float4* __restrict__ gq, cons
       }
     }
   }
-  grad[int64_t(b) * d.count() + i] = acc;
+  float* out = grad + int64_t(b) * d.count() + i;
+  *out = accumulate ? *out + acc : acc;
 }
 
-__global__ void k_quad_fold(const float4* __restrict__ gq, Dims d, int bm, float* __restrict__ grad) {
+static __global__ void k_quad_fold(const float4* __restrict__ gq, Dims d, int bm, float* __restrict__ grad,
+                                   int accumulate) {
   const int x = int(blockIdx.x * blockDim.x + threadIdx.x), y = int(blockIdx.y * blockDim.y + threadIdx.y);
   if (x >= d.x || y >= d.y) return;
   const int b = int(blockIdx.z) / d.z, z = int(blockIdx.z) - b * d.z;
-  quad_fold_at(gq, d, bm, grad, x, y, z, b);
+  quad_fold_at(gq, d, bm, grad, x, y, z, b, accumulate != 0);
 }
 
 }  // namespace ngt

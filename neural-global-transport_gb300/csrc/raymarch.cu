@@ -1179,6 +1179,8 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   if (!a->output_grad || !a->input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: null pointer");
   if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: invalid grad_mode");
+  if (a->accumulate && a->grad_mode != NGT_GRAD_EXACT)
+    return fail(NGT_ERR_UNSUPPORTED, "raymarch_bwd: accumulate needs the exact gradient");
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: the forward output is required");
   if ((rc = check_prepared_quad(&a->fwd))) return rc;
   const Layout l = bwd_layout(a);
@@ -1222,7 +1224,7 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
       p.qd = QuadDims::of(p.din);
       if (cudaMemsetAsync(p.gquad, 0, gquad_bytes(&a->fwd), st) != cudaSuccess)
         return check_launch("raymarch_bwd memset");
-    } else if (cudaMemsetAsync(a->input_grad, 0, size_t(p.N) * vox * cin * cs, st) != cudaSuccess) {
+    } else if (!a->accumulate && cudaMemsetAsync(a->input_grad, 0, size_t(p.N) * vox * cin * cs, st) != cudaSuccess) {
       return check_launch("raymarch_bwd memset");
     }
     if (bl) {
@@ -1239,7 +1241,8 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
     if (quad) {
       CellLaunch fl = cell_launch(p.din);
       fl.grid.z = unsigned(p.din.z * p.N);
-      k_quad_fold<<<fl.grid, fl.block, 0, st>>>(p.gquad, p.din, p.bm, static_cast<float*>(a->input_grad));
+      k_quad_fold<<<fl.grid, fl.block, 0, st>>>(p.gquad, p.din, p.bm, static_cast<float*>(a->input_grad),
+                                                a->accumulate);
     }
     return check_launch("ngt_raymarch_bwd");
   }
@@ -1458,8 +1461,10 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
     const ngt_raymarch_grad_args& g = items[i];
     if (!g.output || !g.output_grad || !g.input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null pointer");
     if (g.fwd.quad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: builds its own quad layouts");
-    if (g.grad_mode != NGT_GRAD_EXACT || g.fwd.blending_mode != NGT_BEER_LAMBERT || g.fwd.interpolation != NGT_LINEAR)
-      return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: exact Beer-Lambert gradients of LINEAR sampling");
+    if (g.grad_mode != NGT_GRAD_EXACT || g.fwd.blending_mode != NGT_BEER_LAMBERT || g.fwd.interpolation != NGT_LINEAR ||
+        g.accumulate)
+      return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: exact Beer-Lambert gradients of LINEAR sampling, "
+                                       "written");
     ptrs[i] = &g.fwd;
   }
   cudaStream_t st = as_stream(stream);

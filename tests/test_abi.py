@@ -207,3 +207,38 @@ def test_nvtx_ranges_wrap_calls(monkeypatch, lib):
     with pytest.raises(L.NGTError):
         L.call("ngt_advect_maccormack_fwd", None, None)
     assert events == [("push", "ngt_raymarch_fwd"), ("pop",), ("push", "ngt_advect_maccormack_fwd"), ("pop",)]
+
+
+def test_accumulate_validation(lib):
+    from ngt_gb300 import _lib as L
+    p = ctypes.c_void_p(0x1000)
+    r = L.RaymarchArgs()
+    r.dtype = L.F32
+    r.input_shape = L.I64x5(1, 4, 4, 4, 1)
+    r.output_dhw = L.I64x3(4, 4, 4)
+    for f in ("input", "output", "matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(r, f, p)
+    r.num_cameras = 1
+    r.interpolation, r.boundary, r.blending_mode, r.separate_camera_batch = 1, 0, 0, 1
+    g = L.RaymarchGradArgs()
+    g.fwd = r
+    g.output = g.output_grad = g.input_grad = p
+    g.grad_mode, g.accumulate = L.GRAD["reference"], 1
+    assert lib.ngt_raymarch_bwd(ctypes.byref(g), None) == L.NGT_ERR_UNSUPPORTED
+    g.grad_mode = L.GRAD["exact"]
+    assert lib.ngt_raymarch_bwd_batch(ctypes.byref(g), 1, 0, p, 1 << 20, None) == L.NGT_ERR_UNSUPPORTED
+    a = L.AdvectArgs()
+    a.dtype = L.F32
+    a.grid_dhw = L.I64x3(4, 4, 4)
+    a.channels = 1
+    for f in ("data", "vel_x", "vel_y", "vel_z", "output", "fwd_field"):
+        setattr(a, f, p)
+    a.order, a.clamp, a.boundary = 2, 1, 1
+    ag = L.AdvectGradArgs()
+    ag.fwd = a
+    ag.output_grad = ag.data_grad = p
+    ag.accumulate, ag.deterministic = 1, 1
+    assert lib.ngt_advect_maccormack_bwd(ctypes.byref(ag), None) == L.NGT_ERR_UNSUPPORTED
+    ag.deterministic = 0
+    ag.vel_x_grad = ag.vel_y_grad = ag.vel_z_grad = p
+    assert lib.ngt_advect_maccormack_bwd_batch(ctypes.byref(ag), 1, p, 1 << 20, None) == L.NGT_ERR_UNSUPPORTED

@@ -662,6 +662,65 @@ def test_advect_stored_mask_matches_recomputed(bm):
         assert rel(N(y), N(x)) < 1e-6
 
 
+@pytest.mark.parametrize("C,emission", [(1, (0.6, 1.2)), (2, None), (1, None)])
+def test_raymarch_backward_accumulates(C, emission):
+    """accumulate = 1 adds the exact input gradient to what input_grad holds
+    (quad layout and direct paths)."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    ops = ngt()
+    lib = L.load()
+    M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
+    x = T((RNG.uniform(0, 1, (1, 10, 12, 14, C)) * 0.3).astype(np.float32))
+    Md, Vd, Pd, Fd = (ops._floats(m, w, x.device) for m, w in ((M, 16), (V, 16), (P, 16), (F, 6)))
+    attrs = dict(interpolation="LINEAR", boundary="CLAMP", blending_mode="BEER_LAMBERT", keep_dims=False,
+                 separate_camera_batch=True, emission_scale=emission)
+    y, _ = ops._ray_forward(x, Md, Vd, Pd, Fd, [10, 8, 6], attrs)
+    gy = T(RNG.standard_normal(tuple(y.shape)).astype(np.float32))
+    want = ops._ray_backward(x, y, gy, Md, Vd, Pd, Fd, [10, 8, 6], attrs, "exact")
+    base = T(RNG.standard_normal(tuple(want.shape)).astype(np.float32))
+    got = base.clone()
+    for _ in range(2):
+        g = L.RaymarchGradArgs()
+        g.fwd = ops._ray_args(x, Md, Vd, Pd, Fd, [10, 8, 6], None, attrs)
+        g.output, g.output_grad, g.input_grad, g.grad_mode = ops._ptr(y), ops._ptr(gy), ops._ptr(got), L.GRAD["exact"]
+        g.accumulate = 1
+        ws = torch.empty(int(lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g))) + 1, dtype=torch.uint8,
+                         device="cuda")
+        g.workspace, g.workspace_bytes = ops._ptr(ws), ws.numel()
+        assert lib.ngt_raymarch_bwd(ctypes.byref(g), ops._stream()) == L.NGT_OK
+    torch.cuda.synchronize()
+    assert rel(N(base + 2 * want), N(got)) < 1e-5
+
+
+@pytest.mark.parametrize("order,clamp", [(2, "MC_SMOOTH"), (1, "NEGATIVE"), (2, "NONE")])
+def test_advect_backward_accumulates(order, clamp):
+    import ctypes
+    from ngt_gb300 import _lib as L
+    from ngt_gb300 import advect
+    ops = ngt()
+    lib = L.load()
+    rho, ux, uy, uz = advect_inputs(shape=(9, 10, 11), seed=41)
+    ts = [T(a) for a in (rho, ux, uy, uz)]
+    out, fwd, mask = advect.warp_forward(*ts, order=order, clamp=clamp, keep_mask=True)
+    gy = T(RNG.standard_normal(tuple(out.shape)).astype(np.float32))
+    want = advect.warp_backward(*ts, fwd, gy, order=order, clamp=clamp, mask=mask)
+    base = [T(RNG.standard_normal(tuple(w.shape)).astype(np.float32)) for w in want]
+    got = [b.clone() for b in base]
+    g = L.AdvectGradArgs()
+    g.fwd = advect._args(*ts, None, fwd, 1.0, order, clamp, "CLAMP", mask)
+    g.output_grad = ops._ptr(gy)
+    g.data_grad, g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (ops._ptr(t) for t in got)
+    g.grad_mode, g.accumulate = L.GRAD["exact"], 1
+    ws = torch.empty(int(lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g))), dtype=torch.uint8,
+                     device="cuda")
+    g.workspace, g.workspace_bytes = ops._ptr(ws), ws.numel()
+    assert lib.ngt_advect_maccormack_bwd(ctypes.byref(g), ops._stream()) == L.NGT_OK
+    torch.cuda.synchronize()
+    for b, w, a in zip(base, want, got):
+        assert rel(N(b + w), N(a)) < 1e-5
+
+
 # ------------------------------------------------------------- unprojection
 @pytest.mark.parametrize("mode", ["reference", "exact"])
 def test_unproject_and_its_gradient(mode):
