@@ -383,7 +383,7 @@ def e2e_measure(torch, dev, w, st, tgt, args, flush):
         ts = [t.to(dev, non_blocking=True).requires_grad_() for t in host]
         r2 = advect.warp(ts[0], ts[1], ts[2], ts[3], dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP")
         img = ops.raymarch_grid_transform(r2[None], w.M, w.V, w.P, w.F, w.image_dhw, emission_scale=scale)
-        loss = 0.5 * ((img[..., :1] - tgt) ** 2).sum()
+        loss = ops.image_l2_loss(img, tgt)
         loss.backward()
         return float(loss.item())
 
@@ -399,7 +399,8 @@ def e2e_measure(torch, dev, w, st, tgt, args, flush):
         one()
         tot += time.perf_counter() - t0
     return {"value": n / tot, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
-            "path": "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + torch loss.backward()"}
+            "path": "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + ops.image_l2_loss, "
+                    "loss.backward()"}
 
 
 def e2e_step_measure(torch, step, w, st, args, flush):

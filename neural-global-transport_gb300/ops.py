@@ -607,3 +607,37 @@ def reduce_grid_blend_grad(output_grad, output, input, blending_mode="BEER_LAMBE
     input = _cuda(input, "input")
     return _rb_backward(_cuda(output_grad, "output_grad").to(input.dtype), _cuda(output, "output").to(input.dtype),
                         input, blending_mode, keep_dims, grad_mode or get_gradient_mode())
+
+
+# ------------------------------------------------------------------ image loss
+class _ImageL2Loss(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, image, target, loss_channels):
+        grad = torch.empty_like(image)
+        loss = torch.zeros((1,), dtype=image.dtype, device=image.device)
+        C = image.shape[-1]
+        L.call("ngt_image_l2_loss", _code(image), image.numel() // C, C, int(loss_channels), _ptr(image),
+               _ptr(target), _ptr(grad), _ptr(loss), _stream())
+        ctx.save_for_backward(grad)
+        return loss[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        grad, = ctx.saved_tensors
+        return grad * g, None, None
+
+
+def image_l2_loss(image, target, loss_channels=1):
+    """0.5 * sum over pixels of (image[..., c] - target[..., c])^2 for the first
+    ``loss_channels`` channels of ``image`` (loss_dens_target on the rendered
+    light channel, optimization.py:478), one kernel that also forms the image
+    gradient; differentiable w.r.t. ``image``.  ``target`` holds
+    ``loss_channels`` channels per pixel.  Float32 or float64 images."""
+    image = _cuda(image, "image")
+    if image.dtype not in (torch.float32, torch.float64):
+        raise TypeError("image_l2_loss: images are float32 or float64")
+    target = _cuda(target, "target").to(image.dtype)
+    C = image.shape[-1]
+    if not 0 < int(loss_channels) <= C or target.numel() != image.numel() // C * int(loss_channels):
+        raise ValueError("image_l2_loss: target must hold loss_channels (1..%d) values per pixel" % C)
+    return _ImageL2Loss.apply(image, target, int(loss_channels))

@@ -721,6 +721,22 @@ def test_advect_backward_accumulates(order, clamp):
         assert rel(N(b + w), N(a)) < 1e-5
 
 
+@pytest.mark.parametrize("dt", [torch.float32, torch.float64])
+def test_image_l2_loss_op(dt):
+    ops = ngt()
+    img = torch.as_tensor(RNG.uniform(0, 1, (1, 3, 8, 6, 2)), device="cuda", dtype=dt).requires_grad_()
+    tgt = torch.as_tensor(RNG.uniform(0, 1, (1, 3, 8, 6, 1)), device="cuda", dtype=dt)
+    loss = ops.image_l2_loss(img, tgt)
+    want = 0.5 * ((img[..., :1] - tgt) ** 2).sum()
+    assert abs(float(loss.detach()) - float(want.detach())) <= 1e-6 * float(want.detach())
+    loss.backward(torch.tensor(2.0, device="cuda", dtype=dt))
+    gw = torch.zeros_like(img)
+    gw[..., :1] = 2.0 * (img[..., :1] - tgt)
+    assert torch.allclose(img.grad, gw.detach(), rtol=1e-6, atol=1e-7)
+    with pytest.raises(ValueError):
+        ops.image_l2_loss(img, tgt.expand(1, 3, 8, 6, 2).contiguous(), loss_channels=1)
+
+
 # ------------------------------------------------------------- unprojection
 @pytest.mark.parametrize("mode", ["reference", "exact"])
 def test_unproject_and_its_gradient(mode):
