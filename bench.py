@@ -133,6 +133,10 @@ class ClockSampler:
 # kernels, from one ncu capture of this workload in f32 (cold cache per kernel):
 # profiles/step_f32_128cube_5views_kernels.md
 NCU_TRAFFIC_F32 = {"raymarch_bwd": 107.90e6}
+# The resource that does bound that call's main kernel (k_raymarch_bwd_bl), from the
+# same capture: L1TEX throughput, driven by its quad gathers and vector atomics.
+NCU_LIMITER_F32 = {"raymarch_bwd": {"resource": "L1TEX (quad gathers + float4 atomics)", "pct_of_peak": 79.8,
+                                    "source": "ncu --set full, profiles/step_f32_128cube_5views_kernels.md"}}
 
 
 def measured_peak_hbm():
@@ -316,6 +320,8 @@ def gpu_arm(args, world, rank, local):
                             "frac": achieved / peak, "peak_kind": peak_kind,
                             "traffic": NCU_TRAFFIC_F32.get(name) if args.dtype == "f32" else None,
                             "algorithmic_bytes_per_launch": nbytes, "avg_ms": avg_ms}
+        if args.dtype == "f32" and name in NCU_LIMITER_F32:
+            line["roofline"]["measured_limiter"] = NCU_LIMITER_F32[name]
     if clk:
         line["clocks"] = clk
     line["e2e"] = e2e
