@@ -401,6 +401,12 @@ int ngt_raymarch_fwd_batch(const ngt_raymarch_args* scenes, int32_t count, int32
                            size_t workspace_bytes, void* stream);
 int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* scenes, int32_t count, int32_t blocks_per_sm,
                            void* workspace, size_t workspace_bytes, void* stream);
+/* ngt_raymarch_bwd_batch for the scenes whose ngt_raymarch_fwd_batch ran last on
+ * this workspace (same arguments, inputs unchanged since): the quad layouts and
+ * extinction-sign words that forward left in the workspace are used instead of
+ * being built again.  No counterpart in the reference. */
+int ngt_raymarch_bwd_batch_after_fwd(const ngt_raymarch_grad_args* scenes, int32_t count, int32_t blocks_per_sm,
+                                     void* workspace, size_t workspace_bytes, void* stream);
 
 /* Density warps of many grids: one launch per phase over the concatenated z
  * planes.  The backward takes exact, non-deterministic gradients with all three

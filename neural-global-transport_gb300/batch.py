@@ -134,9 +134,11 @@ class BatchedScenes:
         self._call("ngt_raymarch_fwd_batch", self.ray, self.n, self.blocks_per_sm[0], _ptr(self.ray_ws),
                    self.ray_ws.numel(), s)
 
-    def render_bwd(self, s):
-        self._call("ngt_raymarch_bwd_batch", self.ray_g, self.n, self.blocks_per_sm[1], _ptr(self.ray_ws),
-                   self.ray_ws.numel(), s)
+    def render_bwd(self, s, after_fwd=True):
+        """The batched render backward; ``after_fwd``: right after render_fwd on the
+        same workspace, whose quad layouts and sign words it reuses."""
+        name = "ngt_raymarch_bwd_batch_after_fwd" if after_fwd else "ngt_raymarch_bwd_batch"
+        self._call(name, self.ray_g, self.n, self.blocks_per_sm[1], _ptr(self.ray_ws), self.ray_ws.numel(), s)
 
     def advect_bwd(self, s):
         self._call("ngt_advect_maccormack_bwd_batch", self.adv_g, self.n, _ptr(self.adv_ws), self.adv_ws.numel(), s)

@@ -1444,7 +1444,8 @@ extern "C" int ngt_raymarch_fwd_batch(const ngt_raymarch_args* items, int32_t co
   if (rc) return rc;
   if (cudaMemsetAsync(workspace, 0, 256, st) != cudaSuccess) return check_launch("raymarch batch memset");
   if (bp.item[0].quad) {
-    rc = build_quads_batch(items[0].dtype, bp, 0, cb, st);
+    // with the extinction-sign words, for ngt_raymarch_bwd_batch_after_fwd
+    rc = build_quads_batch(items[0].dtype, bp, 1, cb, st);
     if (rc) return rc;
   }
   rc = launch_batch_dtype(items[0].dtype, FWD, cin, cb, persistent_blocks(blocks_per_sm, bp.total), st, bp);
@@ -1452,8 +1453,9 @@ extern "C" int ngt_raymarch_fwd_batch(const ngt_raymarch_args* items, int32_t co
   return check_launch("ngt_raymarch_fwd_batch");
 }
 
-extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32_t blocks_per_sm,
-                                      void* workspace, size_t workspace_bytes, void* stream) {
+namespace {
+int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32_t blocks_per_sm, void* workspace,
+                       size_t workspace_bytes, void* stream, bool reuse) {
   if (!items) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null scenes");
   if (count < 1 || count > kMaxBatch) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: 1 to %d scenes", kMaxBatch);
   const ngt_raymarch_args* ptrs[kMaxBatch];
@@ -1483,7 +1485,9 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
     if (!quad && cudaMemsetAsync(p.in_grad, 0, size_t(p.N) * p.din.count() * cin * sizeof(float), st) != cudaSuccess)
       return check_launch("raymarch batch memset");
   }
-  if (cudaMemsetAsync(workspace, 0, 256, st) != cudaSuccess) return check_launch("raymarch batch memset");
+  // the work counter; the sign words too unless the forward's are reused
+  if (cudaMemsetAsync(workspace, 0, (reuse && quad) ? sizeof(int) : 256, st) != cudaSuccess)
+    return check_launch("raymarch batch memset");
   const int dtype = items[0].fwd.dtype;
   if (quad) {
     // quad gradients are contiguous: from the first scene's to the end of the workspace layout
@@ -1491,7 +1495,7 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
     for (int k = 1; k < count; ++k) g0 = std::min(g0, reinterpret_cast<char*>(bp.item[k].gquad));
     const size_t gbytes = batch_bytes(ptrs, count) - size_t(g0 - static_cast<char*>(workspace));
     if (cudaMemsetAsync(g0, 0, gbytes, st) != cudaSuccess) return check_launch("raymarch batch memset");
-    rc = build_quads_batch(dtype, bp, 1, cb, st);
+    rc = reuse ? NGT_OK : build_quads_batch(dtype, bp, 1, cb, st);
   } else {
     rc = launch_batch_dtype(dtype, SIGN, cin, cb, unsigned(sm_count() * 2), st, bp);
   }
@@ -1500,7 +1504,19 @@ extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32
   rc = launch_batch_dtype(dtype, BWD_BL, cin, cb, blocks, st, bp);
   if (rc) return rc;
   if (quad) k_quad_fold_batch<<<unsigned(bp.cblock_end[count - 1]), dim3(32, 8), 0, st>>>(bp);
-  return check_launch("ngt_raymarch_bwd_batch");
+  return check_launch(reuse ? "ngt_raymarch_bwd_batch_after_fwd" : "ngt_raymarch_bwd_batch");
+}
+}  // namespace
+
+extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32_t blocks_per_sm,
+                                      void* workspace, size_t workspace_bytes, void* stream) {
+  return raymarch_bwd_batch(items, count, blocks_per_sm, workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int ngt_raymarch_bwd_batch_after_fwd(const ngt_raymarch_grad_args* items, int32_t count,
+                                                int32_t blocks_per_sm, void* workspace, size_t workspace_bytes,
+                                                void* stream) {
+  return raymarch_bwd_batch(items, count, blocks_per_sm, workspace, workspace_bytes, stream, true);
 }
 
 // ------------------------------------------ backward without caller memory

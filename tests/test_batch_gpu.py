@@ -122,3 +122,23 @@ def test_autotune_and_graph():
     torch.cuda.synchronize()
     for a, c in zip(b.gradients(0), g0):
         assert rel(a, c) < 1e-5
+
+
+def test_backward_reuses_forward_quads():
+    """The batched render backward that reuses the forward's quad layouts and
+    sign words equals the one that builds its own, with a scene whose
+    extinction can be negative among them."""
+    import ctypes
+    _, sc = scenes(n=4, seed=17, signed=(2,))
+    from ngt_gb300.batch import BatchedScenes
+    b = BatchedScenes(sc)
+    b.launch()
+    torch.cuda.synchronize()
+    got = [[g.clone() for g in b.gradients(k)] for k in range(b.n)]
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    b.render_bwd(s, after_fwd=False)
+    b.advect_bwd(s)
+    torch.cuda.synchronize()
+    for k in range(b.n):
+        for a, c in zip(got[k], b.gradients(k)):
+            assert rel(a, c) < 1e-6
