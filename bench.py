@@ -149,6 +149,15 @@ def measured_peak_hbm():
 
 
 # ------------------------------------------------------------------- CPU legs
+_CPU_INPUTS = {}  # per process: inputs of the CPU samples, generated once
+
+
+def _cpu_inputs(key, make):
+    if key not in _CPU_INPUTS:
+        _CPU_INPUTS[key] = make()
+    return _CPU_INPUTS[key]
+
+
 def _cpu_adv_task(n):
     """Advection forward + backward of the oracle on an n^3 grid."""
     sys.path.insert(0, ROOT)
@@ -156,8 +165,8 @@ def _cpu_adv_task(n):
     __graft_entry__.load_package()
     from ngt_gb300 import synthetic
     from oracle import advect
-    rho = synthetic.gaussian_blobs((n, n, n), seed=0)
-    ux, uy, uz = synthetic.curl_noise_mac((n, n, n), max_u=2.0, seed=1)
+    rho, ux, uy, uz = _cpu_inputs(("adv", n), lambda: (synthetic.gaussian_blobs((n, n, n), seed=0),)
+                                  + tuple(synthetic.curl_noise_mac((n, n, n), max_u=2.0, seed=1)))
     t0 = time.perf_counter()
     out = advect.density_maccormack(rho, ux, uy, uz)
     advect.density_maccormack_grad(rho, ux, uy, uz, out)
@@ -171,7 +180,7 @@ def _cpu_render_task(view, rows):
     __graft_entry__.load_package()
     from ngt_gb300 import workloads
     from oracle import ops
-    w = workloads.config2()
+    w = _cpu_inputs("config2", workloads.config2)
     D, H, W = w.image_dhw
     # a band of rows through the image centre: same per-ray work as the full view
     P = w.P[view:view + 1].copy()
@@ -191,21 +200,28 @@ def _cpu_render_task(view, rows):
     return time.perf_counter() - t0
 
 
-def cpu_step_time(processes, adv_n=64, rows=8):
+def cpu_step_time(processes, adv_n=64, rows=8, pool=None):
     """Estimated seconds of one full step on the host: the advection timed on an
     adv_n^3 grid and the render on ``rows`` rows of every view, each scaled
     linearly by its share of the full work; with processes > 1 the render bands
-    run in parallel worker processes (spawned, no CUDA in them)."""
+    run in parallel worker processes (spawned, no CUDA in them; ``pool``: such a
+    pool kept across calls)."""
     import multiprocessing as mp
     full = 128 ** 3
     t_adv = _cpu_adv_task(adv_n) * (full / adv_n ** 3)
     views = 5
     if processes > 1:
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(min(processes, views)) as pool:
+        own = pool is None
+        if own:
+            pool = mp.get_context("spawn").Pool(min(processes, views))
+        try:
             t0 = time.perf_counter()
             pool.starmap(_cpu_render_task, [(v, rows) for v in range(views)])
             t_render_wall = time.perf_counter() - t0
+        finally:
+            if own:
+                pool.close()
+                pool.join()
         # rows of a view are independent: with P processes the full render takes
         # (256/rows) * views bands / P band-times
         per_band = t_render_wall / ((views + min(processes, views) - 1) // min(processes, views))
@@ -216,19 +232,46 @@ def cpu_step_time(processes, adv_n=64, rows=8):
                               "render_sample": "%d of 256 rows per view, 5 views, scaled x%d" % (rows, 256 // rows)}
 
 
+# Wall-clock budget of the reference arm's timed steps (seconds): the per-step
+# sample shrinks with the step count and timing stops once the budget is spent.
+REFERENCE_BUDGET_S = 150.0
+
+
+def reference_sample_plan(calls):
+    """(advection grid side, image rows per view) of each reference step's
+    sample for a run of ``calls`` steps (warm-up included); smaller samples than
+    32^3 and 2 rows are dominated by NumPy call overhead and overstate the
+    scaled step time, so long runs stop at the budget instead."""
+    return (48, 4) if calls <= 10 else (32, 2)
+
+
 def reference_arm(args, world, rank):
     if rank != 0:
         return
+    import multiprocessing as mp
     procs = os.cpu_count() or 1
+    adv_n, rows = reference_sample_plan(args.warmup + args.steps)
     times = []
-    for i in range(args.warmup + args.steps):
-        t, sample = cpu_step_time(procs, adv_n=48, rows=4)
-        if i >= args.warmup:
-            times.append(t)
+    # one worker pool for all steps (a single step makes its own)
+    pool = mp.get_context("spawn").Pool(min(procs, 5)) if procs > 1 and args.warmup + args.steps > 1 else None
+    try:
+        t_begin = time.perf_counter()
+        for i in range(args.warmup + args.steps):
+            if i == args.warmup:
+                t_begin = time.perf_counter()
+            t, sample = cpu_step_time(procs, adv_n=adv_n, rows=rows, pool=pool)
+            if i >= args.warmup:
+                times.append(t)
+                if time.perf_counter() - t_begin > REFERENCE_BUDGET_S:
+                    break
+    finally:
+        if pool is not None:
+            pool.close()
+            pool.join()
     value = 1.0 / float(np.mean(times))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "steps": args.steps, "steps_timed": len(times), "warmup": args.warmup, "ms_per_step": 1e3 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": [128, 128, 128], "views": 5, "image": [256, 256],
                        "depth_samples": 128},
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": procs, "kind": "port",
