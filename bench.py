@@ -41,10 +41,11 @@ def parse():
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--cpu-baseline", default="on", choices=["on", "off"])
     ap.add_argument("--kernel-stats", default="on", choices=["on", "off"])
-    ap.add_argument("--workload", default="step", choices=["step", "chain", "large", "batch"],
+    ap.add_argument("--workload", default="step", choices=["step", "chain", "large", "batch", "velocity"],
                     help="step: the headline differentiated step; chain: the checkpointed 120-frame plume "
                          "chain; large: 256x448x256 grid, 8 views at 512x512x256, 16-bit storage errors; "
-                         "batch: 32 uneven scenes in one batched step")
+                         "batch: 32 uneven scenes in one batched step; velocity: MAC velocity "
+                         "self-advection at 128^3")
     ap.add_argument("--checkpoint-every", type=int, default=10)
     return ap.parse_args()
 
@@ -651,6 +652,81 @@ def batch_arm(args, local):
     print(json.dumps(line), flush=True)
 
 
+def velocity_arm(args, local):
+    """MAC velocity self-advection (``VelocityGrid.warped``: every face component
+    MacCormack-advected on its own lattice by the velocity resampled there) at
+    128^3, forward and backward through the C ABI as one CUDA graph, against the
+    oracle's NumPy restatement on one host core (a 32^3 sample scaled by cells)."""
+    import ctypes
+    import torch
+    import __graft_entry__
+    __graft_entry__.load_package()
+    from ngt_gb300 import _build, _lib as L, synthetic
+    from ngt_gb300.ops import _ptr
+    from oracle import advect as oadvect
+    _build.build_library()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    st = {"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[args.dtype]
+    n = 128
+    u = [torch.as_tensor(a, device=dev).to(st).contiguous()
+         for a in synthetic.curl_noise_mac((n, n, n), max_u=2.0, seed=1)]
+    outs = [torch.empty_like(t) for t in u]
+    fwds = [torch.empty(t.shape, dtype=torch.float32, device=dev) for t in u]
+    rng = np.random.default_rng(5)
+    gout = [torch.as_tensor(rng.standard_normal(tuple(t.shape)).astype(np.float32), device=dev) for t in u]
+    gin = [torch.empty(t.shape, dtype=torch.float32, device=dev) for t in u]
+    a = L.AdvectVelocityArgs()
+    a.dtype = {torch.float32: L.F32, torch.bfloat16: L.BF16, torch.float16: L.F16}[st]
+    a.grid_dhw = L.I64x3(n, n, n)
+    a.vel_x, a.vel_y, a.vel_z = (_ptr(t) for t in u)
+    a.dt, a.order, a.clamp, a.boundary = 1.0, 2, L.CLAMP["MC_SMOOTH"], L.BOUNDARY["CLAMP"]
+    a.out_x, a.out_y, a.out_z = (_ptr(t) for t in outs)
+    a.fwd_x, a.fwd_y, a.fwd_z = (_ptr(t) for t in fwds)
+    g = L.AdvectVelocityGradArgs()
+    g.fwd = a
+    g.grad_x, g.grad_y, g.grad_z = (_ptr(t) for t in gout)
+    g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (_ptr(t) for t in gin)
+    g.grad_mode = L.GRAD["exact"]
+    lib = L.load()
+    ws = torch.empty(int(lib.ngt_advect_velocity_bwd_workspace_bytes(ctypes.byref(g))), dtype=torch.uint8,
+                     device=dev)
+    g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
+
+    def launch():
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L.call("ngt_advect_velocity_fwd", ctypes.byref(a), s)
+        L.call("ngt_advect_velocity_bwd", ctypes.byref(g), s)
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        launch()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        launch()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    ms = _timed(torch, graph.replay, args.steps, max(args.warmup, 3), flush)
+    # the oracle on one core, a 32^3 sample scaled by the cell count
+    m = 32
+    uc = synthetic.curl_noise_mac((m, m, m), max_u=2.0, seed=1)
+    t0 = time.perf_counter()
+    outs_o = oadvect.velocity_maccormack(*uc)
+    oadvect.velocity_maccormack_grad(*uc, outs_o)
+    t_cpu = (time.perf_counter() - t0) * (n / m) ** 3
+    line = {"metric": "MAC velocity self-advection fwd+bwd steps/s at 128^3", "value": 1e3 / ms, "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+            "higher_is_better": True, "dtype": args.dtype, "data": "synthetic (seeded curl-noise MAC velocity)",
+            "config": {"workload": "MacCormack (MC_SMOOTH, CLAMP, dt=1) of the three face grids of a 128^3 MAC "
+                                   "velocity on their own lattices, forward + backward", "cuda_graph": True,
+                       "l2": "flushed between timed steps"},
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": 1, "kind": "port",
+                             "sample": "oracle (NumPy fp32, one process): 32^3 grid, scaled x%d" % (n // m) ** 3}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_init(args)
@@ -662,6 +738,8 @@ def main():
         large_arm(args, local)
     elif args.workload == "batch":
         batch_arm(args, local)
+    elif args.workload == "velocity":
+        velocity_arm(args, local)
     else:
         gpu_arm(args, world, rank, local)
     if world > 1:
