@@ -683,6 +683,11 @@ def velocity_arm(args, local):
     a.dt, a.order, a.clamp, a.boundary = 1.0, 2, L.CLAMP["MC_SMOOTH"], L.BOUNDARY["CLAMP"]
     a.out_x, a.out_y, a.out_z = (_ptr(t) for t in outs)
     a.fwd_x, a.fwd_y, a.fwd_z = (_ptr(t) for t in fwds)
+    # per component: the stored lookup, the MC_SMOOTH revert mask, the corner extrema
+    scratch = [(torch.empty(tuple(t.shape) + (3,), device=dev), torch.empty(t.shape, dtype=torch.uint8, device=dev),
+                torch.empty(tuple(t.shape) + (2,), device=dev)) for t in u]
+    for c, (lut, mask, ext) in enumerate(scratch):
+        a.lookup[c], a.mask[c], a.extrema[c] = _ptr(lut), _ptr(mask), _ptr(ext)
     g = L.AdvectVelocityGradArgs()
     g.fwd = a
     g.grad_x, g.grad_y, g.grad_z = (_ptr(t) for t in gout)

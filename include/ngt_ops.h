@@ -364,6 +364,16 @@ typedef struct {
   void* fwd_x;                /* per-component fwd fields (compute type), kept for the backward */
   void* fwd_y;
   void* fwd_z;
+  /* Optional scratch per face component (x, y, z), kept from the forward to the
+   * backward like fwd_*: lookup (3 compute-type values per face: the velocity
+   * resampled onto that component's lattice, times -dt), written by forward 1
+   * and read by forward 2 and the backward instead of being resampled again;
+   * mask (the MC_SMOOTH revert mask, 1 byte per face) and extrema (2
+   * compute-type values per face) as in ngt_advect_args.  Null: recomputed.
+   * No reference counterpart. */
+  void* lookup[3];
+  void* mask[3];
+  void* extrema[3];
 } ngt_advect_velocity_args;
 
 typedef struct {

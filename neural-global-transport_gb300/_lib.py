@@ -96,7 +96,8 @@ class AdvectGradArgs(ctypes.Structure):
 class AdvectVelocityArgs(ctypes.Structure):
     _fields_ = [("dtype", c_i32), ("grid_dhw", I64x3), ("vel_x", c_vp), ("vel_y", c_vp), ("vel_z", c_vp),
                 ("dt", c_f32), ("order", c_i32), ("clamp", c_i32), ("boundary", c_i32), ("out_x", c_vp),
-                ("out_y", c_vp), ("out_z", c_vp), ("fwd_x", c_vp), ("fwd_y", c_vp), ("fwd_z", c_vp)]
+                ("out_y", c_vp), ("out_z", c_vp), ("fwd_x", c_vp), ("fwd_y", c_vp), ("fwd_z", c_vp),
+                ("lookup", c_vp * 3), ("mask", c_vp * 3), ("extrema", c_vp * 3)]
 
 
 class AdvectVelocityGradArgs(ctypes.Structure):

@@ -126,7 +126,8 @@ def warp(data, vel_x, vel_y, vel_z, dt=1.0, order=2, clamp="MC_SMOOTH", boundary
 
 
 # --------------------------------------------------------- velocity self-advection
-def _vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary):
+def _vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary, scratch=None):
+    """``scratch``: per component (lookup, mask, extrema) tensors or Nones."""
     a = L.AdvectVelocityArgs()
     a.dtype = _code(vx)
     D, H, W1 = vx.shape
@@ -135,7 +136,24 @@ def _vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary):
     a.dt, a.order, a.clamp, a.boundary = float(dt), int(order), L.CLAMP[clamp], L.BOUNDARY[boundary]
     a.out_x, a.out_y, a.out_z = (_ptr(t) for t in outs)
     a.fwd_x, a.fwd_y, a.fwd_z = (_ptr(t) for t in fwds)
+    if scratch is not None:
+        for c, (lut, mask, ext) in enumerate(scratch):
+            a.lookup[c], a.mask[c], a.extrema[c] = _ptr(lut), _ptr(mask), _ptr(ext)
     return a
+
+
+def _vel_scratch(comps, order, clamp):
+    """Per face component: the stored lookup (3 values per face), and for
+    MacCormack with MC_SMOOTH the revert mask and the corner extrema."""
+    cd = compute_dtype(comps[0])
+    smooth = order == 2 and clamp.upper() == "MC_SMOOTH"
+    out = []
+    for t in comps:
+        lut = torch.empty(tuple(t.shape) + (3,), dtype=cd, device=t.device)
+        mask = torch.empty(t.shape, dtype=torch.uint8, device=t.device) if smooth else None
+        ext = torch.empty(tuple(t.shape) + (2,), dtype=cd, device=t.device) if smooth else None
+        out.append((lut, mask, ext))
+    return out
 
 
 class _WarpVelocity(torch.autograd.Function):
@@ -144,9 +162,11 @@ class _WarpVelocity(torch.autograd.Function):
         cd = compute_dtype(vx)
         outs = [torch.empty_like(t) for t in (vx, vy, vz)]
         fwds = [torch.empty(t.shape, dtype=cd, device=t.device) if order == 2 else None for t in (vx, vy, vz)]
-        L.call("ngt_advect_velocity_fwd", ctypes.byref(_vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary)),
-               _stream())
+        scratch = _vel_scratch((vx, vy, vz), order, clamp)
+        L.call("ngt_advect_velocity_fwd",
+               ctypes.byref(_vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary, scratch)), _stream())
         ctx.save_for_backward(vx, vy, vz, *[f for f in fwds if f is not None])
+        ctx.scratch = scratch
         ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode())
         return tuple(outs)
 
@@ -161,13 +181,14 @@ class _WarpVelocity(torch.autograd.Function):
               for g, t in zip((gx, gy, gz), (vx, vy, vz))]
         outs = [torch.empty(t.shape, dtype=cd, device=t.device) for t in (vx, vy, vz)]
         g = L.AdvectVelocityGradArgs()
-        g.fwd = _vel_args(vx, vy, vz, (None, None, None), fwds, dt, order, clamp, boundary)
+        g.fwd = _vel_args(vx, vy, vz, (None, None, None), fwds, dt, order, clamp, boundary, ctx.scratch)
         g.grad_x, g.grad_y, g.grad_z = (_ptr(t) for t in gs)
         g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (_ptr(t) for t in outs)
         g.grad_mode = L.GRAD[mode]
         ws = _workspace(L.load().ngt_advect_velocity_bwd_workspace_bytes(ctypes.byref(g)), vx.device)
         g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
         L.call("ngt_advect_velocity_bwd", ctypes.byref(g), _stream())
+        ctx.scratch = None
         return outs[0], outs[1], outs[2], None, None, None, None
 
 

@@ -102,6 +102,19 @@ struct FaceLookup {
   }
 };
 
+// The lookup that forward 1 of a face component stored (3 values per face).
+template <class T>
+struct StoredLookup {
+  const CT<T>* lut;
+  Dims d;
+  __device__ __forceinline__ void operator()(int x, int y, int z, CT<T> out[3]) const {
+    const int64_t i = flat(x, y, z, d) * 3;
+    out[0] = lut[i];
+    out[1] = lut[i + 1];
+    out[2] = lut[i + 2];
+  }
+};
+
 // ------------------------------------------------------------ MacCormack core
 template <class T>
 struct McParams {
@@ -119,6 +132,7 @@ struct McParams {
   uint8_t* mask;       // MC_SMOOTH revert mask: written by forward 2, read by backward 1 (optional)
   CT<T>* ext;          // MC_SMOOTH: the forward trace's corner extrema (min, max per cell and channel),
                        //   written by forward 1, read instead of gathered again (optional)
+  CT<T>* lut_out;      // forward 1 also stores its lookup here (3 per cell; optional)
   float dt;            // with gface: the lookup is centred(u) * (-dt)
   Dims d;
   int order, clamp, bm, reference;
@@ -138,6 +152,10 @@ __device__ __forceinline__ void mc_fwd1_at(const McParams<T>& p, const LK& lk, i
   const int64_t i = flat(x, y, z, p.d);
   S lut[3];
   lk(x, y, z, lut);
+  if (p.lut_out) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) p.lut_out[i * 3 + k] = lut[k];
+  }
   S v[C];
   if (p.ext && p.order == 2 && p.clamp == NGT_CLAMP_MC_SMOOTH) {
     // the trilinear value and the corner extrema from one fetch of the eight
@@ -788,6 +806,8 @@ McParams<T> vel_params(const ngt_advect_velocity_args* a, int comp) {
   p.data = static_cast<const T*>(data[comp]);
   p.out = static_cast<T*>(out[comp]);
   p.fwd = static_cast<CT<T>*>(fwd[comp]);
+  p.mask = static_cast<uint8_t*>(a->mask[comp]);
+  p.ext = static_cast<CT<T>*>(a->extrema[comp]);
   p.d = face_dims(cells_of(a->grid_dhw), comp);
   p.order = a->order;
   p.clamp = a->clamp;
@@ -797,7 +817,21 @@ McParams<T> vel_params(const ngt_advect_velocity_args* a, int comp) {
 
 template <class T>
 int vel_fwd(const ngt_advect_velocity_args* a, cudaStream_t st) {
-  for (int c = 0; c < 3; ++c) launch_fwd<1, T>(vel_params<T>(a, c), face_lookup<T>(a, c), st);
+  for (int c = 0; c < 3; ++c) {
+    McParams<T> p = vel_params<T>(a, c);
+    if (!a->lookup[c]) {
+      launch_fwd<1, T>(p, face_lookup<T>(a, c), st);
+      continue;
+    }
+    // forward 1 resamples the lookup once and stores it; forward 2 reads it
+    const CellLaunch l = cell_launch(p.d);
+    p.lut_out = static_cast<CT<T>*>(a->lookup[c]);
+    k_mc_fwd1<1, T, FaceLookup<T>><<<l.grid, l.block, 0, st>>>(p, face_lookup<T>(a, c));
+    p.lut_out = nullptr;
+    if (p.order == 2)
+      k_mc_fwd2<1, T, StoredLookup<T>><<<l.grid, l.block, 0, st>>>(
+          p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup[c]), p.d});
+  }
   return check_launch("ngt_advect_velocity_fwd");
 }
 
@@ -847,7 +881,9 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
     p.buf = buf;
     p.cnt = cnt;
     p.accumulate = 1;
-    int rc = launch_bwd12<1, T>(p, face_lookup<T>(a, c), st);
+    int rc = a->lookup[c]
+                 ? launch_bwd12<1, T>(p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup[c]), p.d}, st)
+                 : launch_bwd12<1, T>(p, face_lookup<T>(a, c), st);
     if (rc) return rc;
     if (reference && (cudaMemsetAsync(buf, 0, size_t(nall) * sizeof(S), st) != cudaSuccess ||
                       cudaMemsetAsync(cnt, 0, size_t(nall) * sizeof(unsigned), st) != cudaSuccess))

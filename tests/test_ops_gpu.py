@@ -737,6 +737,45 @@ def test_image_l2_loss_op(dt):
         ops.image_l2_loss(img, tgt.expand(1, 3, 8, 6, 2).contiguous(), loss_channels=1)
 
 
+@pytest.mark.parametrize("order,clamp", [(2, "MC_SMOOTH"), (2, "NONE"), (1, "NEGATIVE")])
+@pytest.mark.parametrize("bm", ["CLAMP", "WRAP", "BORDER"])
+def test_velocity_advection_stored_lookup(order, clamp, bm):
+    """MAC self-advection with the per-component lookups (and MC_SMOOTH mask and
+    extrema) kept from forward 1 against resampling them in every kernel: the
+    same outputs bit for bit, the same gradients up to atomic order."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    from ngt_gb300 import advect
+    ops = ngt()
+    lib = L.load()
+    _, ux, uy, uz = advect_inputs(shape=(9, 10, 11), seed=43)
+    u = [T(a) for a in (ux, uy, uz)]
+    gin = [T(RNG.standard_normal(t.shape).astype(np.float32)) for t in u]
+    res = []
+    for stored in (False, True):
+        outs = [torch.empty_like(t) for t in u]
+        fwds = [torch.empty_like(t) for t in u]
+        scratch = advect._vel_scratch(u, order, clamp) if stored else None
+        a = advect._vel_args(*u, outs, fwds, 1.0, order, clamp, bm, scratch)
+        assert lib.ngt_advect_velocity_fwd(ctypes.byref(a), ops._stream()) == L.NGT_OK
+        g = L.AdvectVelocityGradArgs()
+        g.fwd = a
+        gu = [torch.empty_like(t) for t in u]
+        g.grad_x, g.grad_y, g.grad_z = (ops._ptr(t) for t in gin)
+        g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (ops._ptr(t) for t in gu)
+        g.grad_mode = L.GRAD["exact"]
+        ws = torch.empty(int(lib.ngt_advect_velocity_bwd_workspace_bytes(ctypes.byref(g))), dtype=torch.uint8,
+                         device="cuda")
+        g.workspace, g.workspace_bytes = ops._ptr(ws), ws.numel()
+        assert lib.ngt_advect_velocity_bwd(ctypes.byref(g), ops._stream()) == L.NGT_OK
+        torch.cuda.synchronize()
+        res.append((outs, gu))
+    for a, b in zip(res[0][0], res[1][0]):
+        assert torch.equal(a, b)
+    for a, b in zip(res[0][1], res[1][1]):
+        assert rel(N(a), N(b)) < 1e-6
+
+
 # ------------------------------------------------------------- unprojection
 @pytest.mark.parametrize("mode", ["reference", "exact"])
 def test_unproject_and_its_gradient(mode):
