@@ -319,6 +319,11 @@ typedef struct {
    * gathering the eight corners again.  Null: gathered again.  No reference
    * counterpart. */
   void* extrema;
+  /* Optional scratch of 3 compute-type values per cell, kept for the backward
+   * like fwd_field: forward 1 stores the lookup (centred velocity times -dt)
+   * there and forward 2 and the backward read it instead of averaging the
+   * faces again.  Null: averaged in every kernel.  No reference counterpart. */
+  void* lookup;
 } ngt_advect_args;
 
 typedef struct {

@@ -84,7 +84,8 @@ class ReduceBlendGradArgs(ctypes.Structure):
 class AdvectArgs(ctypes.Structure):
     _fields_ = [("dtype", c_i32), ("grid_dhw", I64x3), ("channels", c_i32), ("data", c_vp), ("vel_x", c_vp),
                 ("vel_y", c_vp), ("vel_z", c_vp), ("dt", c_f32), ("order", c_i32), ("clamp", c_i32),
-                ("boundary", c_i32), ("output", c_vp), ("fwd_field", c_vp), ("mask", c_vp), ("extrema", c_vp)]
+                ("boundary", c_i32), ("output", c_vp), ("fwd_field", c_vp), ("mask", c_vp), ("extrema", c_vp),
+                ("lookup", c_vp)]
 
 
 class AdvectGradArgs(ctypes.Structure):

@@ -80,6 +80,7 @@ class BatchedScenes:
             a.data, a.vel_x, a.vel_y, a.vel_z = _ptr(rho), _ptr(u[0]), _ptr(u[1]), _ptr(u[2])
             a.dt, a.order, a.clamp, a.boundary = float(dt), int(order), L.CLAMP[clamp], L.BOUNDARY[advect_boundary]
             a.output, a.fwd_field = _ptr(rho_adv), _ptr(fwd)
+            a.lookup = _ptr(keep(torch.empty((D, H, W, 3), dtype=cd, device=dev)))
             if int(order) == 2 and clamp.upper() == "MC_SMOOTH":
                 # the revert mask (forward 2 -> backward 1) and the forward trace's
                 # corner extrema (forward 1 -> forward 2)

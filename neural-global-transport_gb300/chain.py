@@ -73,6 +73,9 @@ class AdvectRenderChain:
         self.seg_mask = torch.empty((K, D, H, W, 1), dtype=torch.uint8, device=dev)
         # forward 1 -> forward 2 corner extrema of every advection (stream-ordered, one buffer)
         self.adv_ext = torch.empty((D, H, W, 2), dtype=cd, device=dev)
+        # the lookup (centred velocity times -dt): the velocity is the same for every
+        # frame, so one buffer serves every frame's forward 2 and backward
+        self.adv_lut = torch.empty((D, H, W, 3), dtype=cd, device=dev)
 
         def advect_args(data, out, fwd, mask=None):
             a = L.AdvectArgs()
@@ -84,6 +87,7 @@ class AdvectRenderChain:
             a.output, a.fwd_field = _ptr(out), _ptr(fwd)
             a.mask = _ptr(mask)
             a.extrema = _ptr(self.adv_ext)
+            a.lookup = _ptr(self.adv_lut)
             return a
 
         # chain forward: cur[t % 2] -> cur[(t + 1) % 2]

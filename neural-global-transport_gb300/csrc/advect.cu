@@ -707,7 +707,19 @@ CenteredLookup<T> centered(const ngt_advect_args* a) {
 
 template <int C, class T>
 int density_fwd(const ngt_advect_args* a, cudaStream_t st) {
-  launch_fwd<C, T>(density_params<T>(a), centered<T>(a), st);
+  McParams<T> p = density_params<T>(a);
+  if (!a->lookup) {
+    launch_fwd<C, T>(p, centered<T>(a), st);
+  } else {
+    // forward 1 averages the faces once and stores the lookup; forward 2 reads it
+    const CellLaunch l = cell_launch(p.d);
+    p.lut_out = static_cast<CT<T>*>(a->lookup);
+    k_mc_fwd1<C, T, CenteredLookup<T>><<<l.grid, l.block, 0, st>>>(p, centered<T>(a));
+    p.lut_out = nullptr;
+    if (p.order == 2)
+      k_mc_fwd2<C, T, StoredLookup<T>><<<l.grid, l.block, 0, st>>>(
+          p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup), p.d});
+  }
   return check_launch("ngt_advect_maccormack_fwd");
 }
 
@@ -743,7 +755,9 @@ int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
     p.gface[2] = static_cast<S*>(g->vel_z_grad);
     p.dt = g->fwd.dt;
   }
-  int rc = launch_bwd12<C, T>(p, centered<T>(&g->fwd), st);
+  int rc = g->fwd.lookup
+               ? launch_bwd12<C, T>(p, StoredLookup<T>{static_cast<const CT<T>*>(g->fwd.lookup), p.d}, st)
+               : launch_bwd12<C, T>(p, centered<T>(&g->fwd), st);
   if (rc) return rc;
   if (faces && p.det) {
     const Dims& d = p.d;

@@ -74,6 +74,9 @@ class RenderAdvectStep:
         # forward 1 hands the forward trace's corner extrema to forward 2
         self.mc_ext = torch.empty((D, H, W, 2), dtype=f32, device=dev)
         a.extrema = _ptr(self.mc_ext)
+        # ... and its lookup (centred velocity times -dt) to forward 2 and the backward
+        self.mc_lut = torch.empty((D, H, W, 3), dtype=f32, device=dev)
+        a.lookup = _ptr(self.mc_lut)
         self.adv = a
         ag = L.AdvectGradArgs()
         ag.fwd = a

@@ -619,9 +619,9 @@ def test_advect_backward_deterministic(bm):
 @pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
 @pytest.mark.parametrize("C", [1, 2, 4])
 def test_advect_stored_extrema_bitexact(bm, C):
-    """MacCormack forward with the corner extrema handed from forward 1 to
-    forward 2 against the forward gathering them again: identical outputs,
-    masks and forward fields."""
+    """MacCormack forward with the corner extrema and the lookup handed from
+    forward 1 to forward 2 against the forward forming them again: identical
+    outputs, masks and forward fields."""
     import ctypes
     from ngt_gb300 import _lib as L
     from ngt_gb300 import advect
@@ -636,12 +636,52 @@ def test_advect_stored_extrema_bitexact(bm, C):
         mask = torch.empty(ts[0].shape, dtype=torch.uint8, device="cuda")
         ext = torch.empty(ts[0].shape[:3] + (2 * C,), device="cuda") if with_ext else None
         a = advect._args(*ts, out, fwd, 1.0, 2, "MC_SMOOTH", bm, mask, ext)
+        if with_ext:  # with the stored lookup too
+            lut = torch.empty(ts[0].shape[:3] + (3,), device="cuda")
+            a.lookup = ops._ptr(lut)
         assert L.load().ngt_advect_maccormack_fwd(ctypes.byref(a), ops._stream()) == L.NGT_OK
         torch.cuda.synchronize()
         res.append((out, fwd, mask))
     for a, b in zip(*res):
         assert torch.equal(a, b)
     assert int(res[0][2].sum()) > 0
+
+
+@pytest.mark.parametrize("order,clamp", [(2, "MC_SMOOTH"), (1, "NEGATIVE"), (2, "NONE")])
+def test_advect_backward_stored_lookup(order, clamp):
+    """The MacCormack backward reading the lookup that forward 1 stored against
+    the backward averaging the faces again."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    from ngt_gb300 import advect
+    ops = ngt()
+    lib = L.load()
+    rho, ux, uy, uz = advect_inputs(shape=(9, 10, 11), seed=47)
+    ts = [T(a) for a in (rho, ux, uy, uz)]
+    gy = T(RNG.standard_normal(rho.shape).astype(np.float32))
+    res = []
+    for stored in (False, True):
+        out, fwd = torch.empty_like(ts[0]), torch.empty_like(ts[0])
+        a = advect._args(*ts, out, fwd, 1.0, order, clamp, "CLAMP")
+        lut = torch.empty(ts[0].shape[:3] + (3,), device="cuda")
+        if stored:
+            a.lookup = ops._ptr(lut)
+        assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), ops._stream()) == L.NGT_OK
+        g = L.AdvectGradArgs()
+        g.fwd = a
+        grads = [torch.empty_like(t) for t in ts]
+        g.output_grad = ops._ptr(gy)
+        g.data_grad, g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (ops._ptr(t) for t in grads)
+        g.grad_mode = L.GRAD["exact"]
+        ws = torch.empty(int(lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g))), dtype=torch.uint8,
+                         device="cuda")
+        g.workspace, g.workspace_bytes = ops._ptr(ws), ws.numel()
+        assert lib.ngt_advect_maccormack_bwd(ctypes.byref(g), ops._stream()) == L.NGT_OK
+        torch.cuda.synchronize()
+        res.append((out, grads))
+    assert torch.equal(res[0][0], res[1][0])
+    for a_, b_ in zip(res[0][1], res[1][1]):
+        assert rel(N(a_), N(b_)) < 1e-6
 
 
 @pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
