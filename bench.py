@@ -133,11 +133,11 @@ class ClockSampler:
 # DRAM bytes (read + write) per call of the dominant library call, summed over its
 # kernels, from one ncu capture of this workload in f32 (cold cache per kernel):
 # profiles/step_f32_128cube_5views_kernels.md
-NCU_TRAFFIC_F32 = {"raymarch_bwd": 107.90e6}
+NCU_TRAFFIC_F32 = {"raymarch_bwd": 108.2e6}
 # The resource that does bound that call's main kernel (k_raymarch_bwd_bl), from the
 # same capture: L1TEX throughput, driven by its quad gathers and vector atomics.
-NCU_LIMITER_F32 = {"raymarch_bwd": {"resource": "L1TEX (quad gathers + float4 atomics)", "pct_of_peak": 79.8,
-                                    "source": "ncu --set full, profiles/step_f32_128cube_5views_kernels.md"}}
+NCU_LIMITER_F32 = {"raymarch_bwd": {"resource": "L1TEX (quad gathers + float4 atomics)", "pct_of_peak": 80.2,
+                                    "source": "ncu sections, profiles/step_f32_128cube_5views_kernels.md"}}
 
 
 def measured_peak_hbm():
