@@ -231,10 +231,20 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
     for (int c = 0; c < C; ++c) s.back[c] = S(0);
   } else {
     tri_fetch<C>(p.fwd, tb, p.d, vb);
-    tri_combine<C>(vb, tb, s.back);
   }
   S mn[C], mx[C];
   const bool recompute = p.clamp == NGT_CLAMP_MC_SMOOTH && !(stored && p.mask);
+  // the backward needs the corrected value only to recompute the mask or for the
+  // NEGATIVE clamp; otherwise only the corners (vb) and the mask
+  if (stored && !recompute && p.clamp != NGT_CLAMP_NEGATIVE) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      s.mask[c] = p.clamp == NGT_CLAMP_MC_SMOOTH && p.mask[i * C + c] != 0;
+      s.fwd[c] = s.back[c] = s.corr[c] = s.res[c] = S(0);
+    }
+    return;
+  }
+  if (!(p.bm == BORDER && !tb.inside)) tri_combine<C>(vb, tb, s.back);
   if (recompute && p.ext) {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
