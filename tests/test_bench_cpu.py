@@ -1,0 +1,78 @@
+"""Host-side pieces of bench.py that need no GPU: the clock-sample parsing, the
+peak lookup, the reference arm's sample plan, and the reference arm's JSON line
+(with a stand-in for the timed CPU step)."""
+import io
+import json
+import os
+import sys
+from contextlib import redirect_stdout
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+class _Done:
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+    def kill(self):
+        pass
+
+
+def test_clock_samples_parsed():
+    c = bench.ClockSampler(0)
+    c.proc = _Done()
+    c.skip = 1
+    c.lines = ["0, 1500, 2070, 300.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+               "0, 2070, 2070, 900.5, 0x4, Not Active, Not Active, Not Active, Active",
+               "0, 2040, 2070, 950.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+               "0, 2070, 2070, 940.0, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    got = c.stop()
+    assert got == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+
+
+def test_clock_sampler_without_samples():
+    c = bench.ClockSampler(0)
+    assert c.stop() is None
+
+
+def test_measured_peak_fallback(tmp_path, monkeypatch):
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert bench.measured_peak_hbm() == (6800.0, "fallback")
+    (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 6798.9}))
+    assert bench.measured_peak_hbm() == (6798.9, "measured")
+
+
+def test_reference_sample_plan():
+    assert bench.reference_sample_plan(5) == (48, 4)
+    assert bench.reference_sample_plan(405) == (32, 2)
+
+
+def test_reference_arm_line(monkeypatch):
+    """The reference arm's line carries the contract's keys, and stops timing at
+    its budget (here: after the first timed step)."""
+    import argparse
+    calls = []
+
+    def fake(procs, adv_n=64, rows=8, pool=None):
+        calls.append((adv_n, rows))
+        return 20.0, {"advect_sample": "a", "render_sample": "r"}
+
+    monkeypatch.setattr(bench, "cpu_step_time", fake)
+    monkeypatch.setattr(bench, "REFERENCE_BUDGET_S", -1.0)
+    monkeypatch.setattr(os, "cpu_count", lambda: 1)
+    buf = io.StringIO()
+    with redirect_stdout(buf):
+        bench.reference_arm(argparse.Namespace(impl="reference", gpus=1, steps=400, warmup=2), 1, 0)
+    line = json.loads(buf.getvalue().strip().splitlines()[-1])
+    assert len(calls) == 3 and calls[0] == (32, 2)
+    assert line["impl"] == "reference" and line["steps"] == 400 and line["steps_timed"] == 1
+    assert abs(line["value"] - 0.05) < 1e-12 and line["unit"] == "steps/s" and line["higher_is_better"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 1
+    assert line["e2e"] == {"value": line["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
