@@ -454,6 +454,9 @@ int ngt_raymarch_fwd_l2(const ngt_raymarch_args* args, const void* target, int32
 /* ------------------------------------------------------------ diagnostics */
 const char* ngt_last_error_message(void);
 int ngt_version(void);
+/* sizeof of the argument struct named ``name`` (e.g. "ngt_raymarch_args"), 0 for
+ * an unknown name: lets a binding check its mirror of the layouts. */
+size_t ngt_struct_size(const char* name);
 
 #ifdef __cplusplus
 }

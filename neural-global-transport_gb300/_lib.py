@@ -148,6 +148,7 @@ SIGNATURES = {
     "ngt_image_l2_loss": ([c_i32, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp], c_i32),
     "ngt_last_error_message": ([], ctypes.c_char_p),
     "ngt_version": ([], c_i32),
+    "ngt_struct_size": ([ctypes.c_char_p], c_sz),
 }
 
 _lib = None

@@ -242,3 +242,22 @@ def test_accumulate_validation(lib):
     ag.deterministic = 0
     ag.vel_x_grad = ag.vel_y_grad = ag.vel_z_grad = p
     assert lib.ngt_advect_maccormack_bwd_batch(ctypes.byref(ag), 1, p, 1 << 20, None) == L.NGT_ERR_UNSUPPORTED
+
+
+def test_struct_layouts_match_the_header(lib):
+    """The ctypes mirrors of the argument structs have the library's sizes (a
+    field added on one side only would shift every field after it)."""
+    from ngt_gb300 import _lib as L
+    mirrors = {"ngt_sample_lut_args": L.SampleLutArgs, "ngt_sample_lut_grad_args": L.SampleLutGradArgs,
+               "ngt_sample_transform_args": L.SampleTransformArgs,
+               "ngt_sample_transform_grad_args": L.SampleTransformGradArgs, "ngt_lod_args": L.LodArgs,
+               "ngt_raymarch_args": L.RaymarchArgs, "ngt_raymarch_grad_args": L.RaymarchGradArgs,
+               "ngt_reduce_blend_args": L.ReduceBlendArgs, "ngt_reduce_blend_grad_args": L.ReduceBlendGradArgs,
+               "ngt_advect_args": L.AdvectArgs, "ngt_advect_grad_args": L.AdvectGradArgs,
+               "ngt_advect_velocity_args": L.AdvectVelocityArgs,
+               "ngt_advect_velocity_grad_args": L.AdvectVelocityGradArgs}
+    text = open(os.path.join(ROOT, "include", "ngt_ops.h")).read()
+    assert set(re.findall(r"} (ngt_\w+_args);", text)) == set(mirrors)
+    for name, cls in mirrors.items():
+        assert lib.ngt_struct_size(name.encode()) == ctypes.sizeof(cls), name
+    assert lib.ngt_struct_size(b"ngt_no_such_args") == 0
