@@ -32,7 +32,7 @@ def _faces(t, name):
     return t.contiguous()
 
 
-def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None, extrema=None):
+def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None, extrema=None, lookup=None):
     a = L.AdvectArgs()
     a.dtype = _code(data)
     D, H, W, C = data.shape
@@ -46,6 +46,7 @@ def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None, ext
     a.output, a.fwd_field = _ptr(out), _ptr(fwd)
     a.mask = _ptr(mask)
     a.extrema = _ptr(extrema)
+    a.lookup = _ptr(lookup)
     return a
 
 
@@ -56,9 +57,12 @@ def _check_faces(data, vx, vy, vz):
                          % (tuple(data.shape), tuple(vx.shape), tuple(vy.shape), tuple(vz.shape)))
 
 
-def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP", keep_mask=False):
+def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP", keep_mask=False,
+                 lookup=None):
     """Forward only; returns (output, fwd_field, mask) with fwd_field and the
-    MC_SMOOTH revert mask (when ``keep_mask``) kept for the backward."""
+    MC_SMOOTH revert mask (when ``keep_mask``) kept for the backward.
+    ``lookup``: optional (D, H, W, 3) compute-type buffer where forward 1 leaves
+    the lookup (centred velocity times -dt) for forward 2 and the backward."""
     out = torch.empty_like(data)
     fwd = torch.empty(data.shape, dtype=compute_dtype(data), device=data.device) if order == 2 else None
     smooth = order == 2 and clamp.upper() == "MC_SMOOTH"
@@ -67,15 +71,16 @@ def warp_forward(data, vx, vy, vz, dt=1.0, order=2, clamp="MC_SMOOTH", boundary=
     ext = torch.empty(data.shape[:3] + (2 * data.shape[3],), dtype=compute_dtype(data),
                       device=data.device) if smooth else None
     L.call("ngt_advect_maccormack_fwd",
-           ctypes.byref(_args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask, ext)), _stream())
+           ctypes.byref(_args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask, ext, lookup)), _stream())
     return out, fwd, mask
 
 
 def warp_backward(data, vx, vy, vz, fwd, grad, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP",
-                  grad_mode=None, velocity_grad=True, deterministic=None, mask=None):
+                  grad_mode=None, velocity_grad=True, deterministic=None, mask=None, lookup=None):
+    """``lookup``: the buffer the forward stored its lookup in, or None."""
     cd = compute_dtype(data)
     g = L.AdvectGradArgs()
-    g.fwd = _args(data, vx, vy, vz, None, fwd, dt, order, clamp, boundary, mask)
+    g.fwd = _args(data, vx, vy, vz, None, fwd, dt, order, clamp, boundary, mask, lookup=lookup)
     gd = torch.empty(data.shape, dtype=cd, device=data.device)
     gx = torch.empty(vx.shape, dtype=cd, device=data.device) if velocity_grad else None
     gy = torch.empty(vy.shape, dtype=cd, device=data.device) if velocity_grad else None
@@ -94,17 +99,21 @@ def warp_backward(data, vx, vy, vz, fwd, grad, dt=1.0, order=2, clamp="MC_SMOOTH
 class _Warp(torch.autograd.Function):
     @staticmethod
     def forward(ctx, data, vx, vy, vz, dt, order, clamp, boundary):
-        out, fwd, mask = warp_forward(data, vx, vy, vz, dt, order, clamp, boundary, keep_mask=True)
-        ctx.save_for_backward(data, vx, vy, vz, fwd, mask)
+        # MacCormack: forward 1 stores the lookup for forward 2 and the backward
+        lut = torch.empty(data.shape[:3] + (3,), dtype=compute_dtype(data), device=data.device) \
+            if order == 2 else None
+        out, fwd, mask = warp_forward(data, vx, vy, vz, dt, order, clamp, boundary, keep_mask=True, lookup=lut)
+        ctx.save_for_backward(data, vx, vy, vz, fwd, mask, lut)
         ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode(), get_deterministic())
         return out
 
     @staticmethod
     def backward(ctx, grad):
-        data, vx, vy, vz, fwd, mask = ctx.saved_tensors
+        data, vx, vy, vz, fwd, mask, lut = ctx.saved_tensors
         dt, order, clamp, boundary, mode, det = ctx.cfg
         gd, gx, gy, gz = warp_backward(data, vx, vy, vz, fwd, grad.contiguous(), dt, order, clamp, boundary, mode,
-                                       velocity_grad=any(ctx.needs_input_grad[1:4]), deterministic=det, mask=mask)
+                                       velocity_grad=any(ctx.needs_input_grad[1:4]), deterministic=det, mask=mask,
+                                       lookup=lut)
         return gd, gx, gy, gz, None, None, None, None
 
 

@@ -124,7 +124,10 @@ def _cache_get(cache, key):
     cache.move_to_end(key)
     index = hit[0].device.index
     if _stream_handle(index) != hit[2]:
-        torch.cuda.current_stream(index).wait_event(hit[1])
+        stream = torch.cuda.current_stream(index)
+        stream.wait_event(hit[1])
+        # an entry evicted while this stream still reads it must not be reused early
+        hit[0].record_stream(stream)
     return hit[0]
 
 

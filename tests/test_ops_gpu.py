@@ -480,6 +480,13 @@ def test_host_matrix_and_camera_caches():
     # moved to the new matrix content: a different image
     y4 = ops.raymarch_grid_transform(x, M2, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
     assert not torch.equal(y1, y4)
+    # a call on another stream reuses the entries made on the default stream
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        y5 = ops.raymarch_grid_transform(x.detach(), M, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
+    torch.cuda.current_stream(dev).wait_stream(side)
+    assert len(ops._CAMERAS) >= n_cams and torch.equal(y1, y5)
 
 
 @pytest.mark.parametrize("bm", ["BORDER", "CLAMP", "WRAP"])
