@@ -88,11 +88,11 @@ __device__ __forceinline__ void slot_to_bc(const RayParams& p, int slot, int& b,
 
 __host__ __device__ __forceinline__ int num_slots_dev(const RayParams& p) { return p.sep ? p.N * p.ncam : p.N; }
 
+// This thread's pixel within its 16x8 tile: each warp covers 8x4 pixels (rays
+// that stay close in the grid, so a warp's gathers share cache lines); warps 0
+// and 1 side by side in x, warps 2 and 3 below them.
 __device__ __forceinline__ void pixel_of_thread(int& px, int& py) {
-  const int t = threadIdx.x;
-  const int lane = t & 31, warp = t >> 5;
-  const int tiles_x = 0;  // unused
-  (void)tiles_x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   px = (warp & 1) * 8 + (lane & 7);
   py = (warp >> 1) * 4 + (lane >> 3);
 }
