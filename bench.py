@@ -30,6 +30,34 @@ METRIC = "fwd+bwd render+advect steps/s at 128^3 x 5 views"
 WORKLOAD = "MacCormack advect (MC_SMOOTH, CLAMP, dt=1) + 5-view Beer-Lambert raymarch 256x256x128 (BORDER) + L2 + backward to density and MAC velocity, 128^3 grid"
 
 
+# Arm CPU parts by MIDR part number (implementer 0x41), for the host description
+_ARM_PARTS = {"0xd40": "Neoverse-V1", "0xd49": "Neoverse-N2", "0xd4f": "Neoverse-V2", "0xd84": "Neoverse-V3",
+              "0xd8e": "Neoverse-N3"}
+
+
+def host_cpu(cpuinfo="/proc/cpuinfo"):
+    """The host the CPU baselines run on: architecture, logical CPUs and the CPU
+    model (``model name`` on x86, the implementer / part words on Arm)."""
+    import platform
+    import re
+    info = {"arch": platform.machine(), "logical_cpus": os.cpu_count()}
+    try:
+        with open(cpuinfo) as f:
+            text = f.read()
+    except OSError:
+        return info
+    m = re.search(r"^model name\s*:\s*(.+)$", text, re.M)
+    if m:
+        info["model"] = m.group(1).strip()
+        return info
+    parts = sorted(set(re.findall(r"^CPU part\s*:\s*(\S+)$", text, re.M)))
+    impl = sorted(set(re.findall(r"^CPU implementer\s*:\s*(\S+)$", text, re.M)))
+    if parts:
+        names = [_ARM_PARTS.get(p, "part " + p) if impl == ["0x41"] else "part " + p for p in parts]
+        info["model"] = ", ".join(names) + (" (implementer %s)" % "/".join(impl) if impl else "")
+    return info
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -277,7 +305,8 @@ def reference_arm(args, world, rank):
                        "depth_samples": 128},
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": procs, "kind": "port",
                              "sample": "NumPy restatement of the reference operators (the reference has no CPU "
-                                       "path); per step: %s; %s" % (sample["advect_sample"], sample["render_sample"])},
+                                       "path); per step: %s; %s" % (sample["advect_sample"], sample["render_sample"]),
+                             "host": host_cpu()},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -375,7 +404,8 @@ def gpu_arm(args, world, rank, local):
         t, sample = cpu_step_time(1, adv_n=48, rows=4)
         line["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": 1, "kind": "port",
                                 "sample": "oracle (NumPy fp32, single process) per step: %s; %s"
-                                          % (sample["advect_sample"], sample["render_sample"])}
+                                          % (sample["advect_sample"], sample["render_sample"]),
+                                "host": host_cpu()}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -728,7 +758,8 @@ def velocity_arm(args, local):
                                    "velocity on their own lattices, forward + backward", "cuda_graph": True,
                        "l2": "flushed between timed steps"},
             "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": 1, "kind": "port",
-                             "sample": "oracle (NumPy fp32, one process): 32^3 grid, scaled x%d" % (n // m) ** 3}}
+                             "sample": "oracle (NumPy fp32, one process): 32^3 grid, scaled x%d" % (n // m) ** 3,
+                             "host": host_cpu()}}
     print(json.dumps(line), flush=True)
 
 

@@ -76,3 +76,20 @@ def test_reference_arm_line(monkeypatch):
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 1
     assert line["e2e"] == {"value": line["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    assert line["cpu_baseline"]["host"]["logical_cpus"] == 1
+
+
+def test_host_cpu_description(tmp_path):
+    x86 = tmp_path / "x86"
+    x86.write_text("processor\t: 0\nmodel name\t: Some CPU @ 2.0GHz\n\nprocessor\t: 1\n"
+                   "model name\t: Some CPU @ 2.0GHz\n")
+    assert bench.host_cpu(str(x86))["model"] == "Some CPU @ 2.0GHz"
+    arm = tmp_path / "arm"
+    arm.write_text("processor\t: 0\nCPU implementer\t: 0x41\nCPU part\t: 0xd4f\n\n"
+                   "processor\t: 1\nCPU implementer\t: 0x41\nCPU part\t: 0xd4f\n")
+    assert bench.host_cpu(str(arm))["model"] == "Neoverse-V2 (implementer 0x41)"
+    other = tmp_path / "other"
+    other.write_text("CPU implementer\t: 0x61\nCPU part\t: 0x022\n")
+    assert bench.host_cpu(str(other))["model"] == "part 0x022 (implementer 0x61)"
+    missing = bench.host_cpu(str(tmp_path / "absent"))
+    assert "model" not in missing and missing["logical_cpus"] >= 1 and missing["arch"]
