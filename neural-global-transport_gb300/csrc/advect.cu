@@ -115,6 +115,15 @@ struct StoredLookup {
   }
 };
 
+// Forward 1 and backward 2 of one channel of 16-bit data with a cell-centred or
+// stored lookup are held to the f32 variants' register counts (32 and 48: 8 and 5
+// resident 256-thread blocks per SM); left to themselves they take 33 and 50 and
+// lose a block per SM.  Every other variant is unbounded (minimum blocks 0).
+template <int C, class T, class LK>
+__host__ __device__ constexpr bool mc_narrow16() {
+  return C == 1 && sizeof(T) == 2 && !std::is_same<LK, FaceLookup<T>>::value;
+}
+
 // ------------------------------------------------------------ MacCormack core
 template <class T>
 struct McParams {
@@ -203,7 +212,7 @@ __device__ __forceinline__ void mc_fwd1_at(const McParams<T>& p, const LK& lk, i
 }
 
 template <int C, class T, class LK>
-__global__ void __launch_bounds__(kBlock) k_mc_fwd1(McParams<T> p, LK lk) {
+__global__ void __launch_bounds__(kBlock, (mc_narrow16<C, T, LK>() ? 8 : 0)) k_mc_fwd1(McParams<T> p, LK lk) {
   int x, y, z;
   if (!launch_cell(p.d, x, y, z)) return;
   mc_fwd1_at<C>(p, lk, x, y, z);
@@ -510,7 +519,7 @@ __device__ __forceinline__ void mc_bwd2_at(const McParams<T>& p, const LK& lk, i
 }
 
 template <int C, class T, class LK>
-__global__ void __launch_bounds__(kBlock) k_mc_bwd2(McParams<T> p, LK lk) {
+__global__ void __launch_bounds__(kBlock, (mc_narrow16<C, T, LK>() ? 5 : 0)) k_mc_bwd2(McParams<T> p, LK lk) {
   int x, y, z;
   const bool active = launch_cell(p.d, x, y, z);
   if (__all_sync(0xffffffffu, !active)) return;
