@@ -12,6 +12,12 @@
  *    Outputs, gradients and any workspace are owned by the caller.  Every
  *    op that needs scratch memory reports its size through the matching
  *    *_workspace_bytes() query.
+ *  - Every buffer starts on a multiple of its element size (the storage type
+ *    for grids, float -- double for NGT_F64 -- for images, gradients and
+ *    scratch fields, float for matrices); workspaces and camera blocks on 16
+ *    bytes, prepared quad layouts on 256.  A misaligned pointer is rejected
+ *    with NGT_ERR_INVALID_ARGUMENT naming it.  (Allocations from cudaMalloc
+ *    or a PyTorch tensor of the element type always qualify.)
  *  - Matrices (model M per batch entry, view V / projection P per camera)
  *    are 16 floats read column-major, exactly the buffer the reference ops
  *    receive (renderer.py:117-121 passes matrix.transpose()); frusta are 6

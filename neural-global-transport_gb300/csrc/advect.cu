@@ -667,7 +667,12 @@ int validate(const ngt_advect_args* a) {
   if (!valid_channels(a->channels)) return fail(NGT_ERR_INVALID_ARGUMENT, "Only 1,2 and 4 Channel supported.");
   if (!a->data || !a->vel_x || !a->vel_y || !a->vel_z) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null pointer");
   if (a->order == 2 && !a->fwd_field) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: MacCormack needs fwd_field");
-  return NGT_OK;
+  if ((rc = check_aligned("advect", storage_bytes(a->dtype), {{"data", a->data}, {"vel_x", a->vel_x},
+                                                              {"vel_y", a->vel_y}, {"vel_z", a->vel_z},
+                                                              {"output", a->output}})))
+    return rc;
+  return check_aligned("advect", arith_bytes(a->dtype),
+                       {{"fwd_field", a->fwd_field}, {"extrema", a->extrema}, {"lookup", a->lookup}});
 }
 
 Dims cells_of(const int64_t* dhw) { return Dims{int(dhw[2]), int(dhw[1]), int(dhw[0])}; }
@@ -814,7 +819,14 @@ int validate_vel(const ngt_advect_velocity_args* a) {
   if (!a->vel_x || !a->vel_y || !a->vel_z) return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity: null pointer");
   if (a->order == 2 && (!a->fwd_x || !a->fwd_y || !a->fwd_z))
     return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity: MacCormack needs the fwd fields");
-  return NGT_OK;
+  if ((rc = check_aligned("advect_velocity", storage_bytes(a->dtype),
+                          {{"vel_x", a->vel_x}, {"vel_y", a->vel_y}, {"vel_z", a->vel_z}, {"out_x", a->out_x},
+                           {"out_y", a->out_y}, {"out_z", a->out_z}})))
+    return rc;
+  return check_aligned("advect_velocity", arith_bytes(a->dtype),
+                       {{"fwd_x", a->fwd_x}, {"fwd_y", a->fwd_y}, {"fwd_z", a->fwd_z}, {"lookup[0]", a->lookup[0]},
+                        {"lookup[1]", a->lookup[1]}, {"lookup[2]", a->lookup[2]}, {"extrema[0]", a->extrema[0]},
+                        {"extrema[1]", a->extrema[1]}, {"extrema[2]", a->extrema[2]}});
 }
 
 template <class T>
@@ -1089,6 +1101,12 @@ extern "C" int ngt_advect_maccormack_bwd(const ngt_advect_grad_args* g, void* st
     return fail(NGT_ERR_INVALID_ARGUMENT, "advect_bwd: invalid grad_mode");
   if (g->accumulate && (g->grad_mode != NGT_GRAD_EXACT || g->deterministic))
     return fail(NGT_ERR_UNSUPPORTED, "advect_bwd: accumulate needs the exact, non-deterministic gradient");
+  if ((rc = check_aligned("advect_bwd", arith_bytes(g->fwd.dtype),
+                          {{"output_grad", g->output_grad}, {"data_grad", g->data_grad},
+                           {"vel_x_grad", g->vel_x_grad}, {"vel_y_grad", g->vel_y_grad},
+                           {"vel_z_grad", g->vel_z_grad}})) ||
+      (rc = check_aligned("advect_bwd", kScratchAlign, {{"workspace", g->workspace}})))
+    return rc;
   const size_t need = ngt_advect_maccormack_bwd_workspace_bytes(g);
   if (!g->workspace || g->workspace_bytes < need)
     return fail(NGT_ERR_WORKSPACE, "advect_bwd needs %zu workspace bytes", need);
@@ -1130,6 +1148,12 @@ extern "C" int ngt_advect_velocity_bwd(const ngt_advect_velocity_grad_args* g, v
     return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity_bwd: null pointer");
   if (g->grad_mode != NGT_GRAD_EXACT && g->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "advect_velocity_bwd: invalid grad_mode");
+  if ((rc = check_aligned("advect_velocity_bwd", arith_bytes(g->fwd.dtype),
+                          {{"grad_x", g->grad_x}, {"grad_y", g->grad_y}, {"grad_z", g->grad_z},
+                           {"vel_x_grad", g->vel_x_grad}, {"vel_y_grad", g->vel_y_grad},
+                           {"vel_z_grad", g->vel_z_grad}})) ||
+      (rc = check_aligned("advect_velocity_bwd", kScratchAlign, {{"workspace", g->workspace}})))
+    return rc;
   const size_t need = ngt_advect_velocity_bwd_workspace_bytes(g);
   if (!g->workspace || g->workspace_bytes < need)
     return fail(NGT_ERR_WORKSPACE, "advect_velocity_bwd needs %zu workspace bytes", need);
@@ -1175,10 +1199,16 @@ extern "C" int ngt_advect_maccormack_bwd_batch(const ngt_advect_grad_args* items
       return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch backward: null pointer");
     if (g.grad_mode != NGT_GRAD_EXACT || g.deterministic || g.accumulate)
       return fail(NGT_ERR_UNSUPPORTED, "advect batch backward: exact, non-deterministic, written gradients only");
+    const int ra = check_aligned("advect batch backward", arith_bytes(g.fwd.dtype),
+                                 {{"output_grad", g.output_grad}, {"data_grad", g.data_grad},
+                                  {"vel_x_grad", g.vel_x_grad}, {"vel_y_grad", g.vel_y_grad},
+                                  {"vel_z_grad", g.vel_z_grad}});
+    if (ra) return ra;
   }
   int zsum, mw, mh;
-  const int rc = validate_batch(a, count, zsum, mw, mh);
+  int rc = validate_batch(a, count, zsum, mw, mh);
   if (rc) return rc;
+  if ((rc = check_aligned("advect batch backward", kScratchAlign, {{"workspace", workspace}}))) return rc;
   const size_t need = batch_bwd_bytes(items, count);
   if (!workspace || workspace_bytes < need)
     return fail(NGT_ERR_WORKSPACE, "advect batch backward needs %zu workspace bytes", need);

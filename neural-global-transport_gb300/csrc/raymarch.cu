@@ -713,6 +713,14 @@ int validate(const ngt_raymarch_args* a, int& cin, int& cb) {
   if (a->dtype < NGT_F32 || a->dtype > NGT_F16) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: invalid dtype");
   if (a->input_shape[1] > (1 << 30) || a->output_dhw[1] * a->output_dhw[2] > (int64_t(1) << 31))
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: shape too large");
+  int rc;
+  if ((rc = check_aligned("raymarch", storage_bytes(a->dtype), {{"input", a->input}})) ||
+      (rc = check_aligned("raymarch", arith_bytes(a->dtype), {{"output", a->output}})) ||
+      (rc = check_aligned("raymarch", sizeof(float), {{"matrix_m", a->matrix_m}, {"matrix_v", a->matrix_v},
+                                                      {"matrix_p", a->matrix_p}, {"frustum", a->frustum}})) ||
+      (rc = check_aligned("raymarch", kScratchAlign, {{"cameras", a->cameras}, {"workspace", a->workspace}})) ||
+      (rc = check_aligned("raymarch", 256, {{"quad", a->quad}})))
+    return rc;
   return NGT_OK;
 }
 
@@ -1159,6 +1167,9 @@ extern "C" int ngt_raymarch_fwd_l2(const ngt_raymarch_args* a, const void* targe
                                    void* image_grad, void* loss, void* stream) {
   if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null arguments");
   if (!target || !image_grad || !loss) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2: null pointer");
+  const int ra = check_aligned("raymarch_fwd_l2", arith_bytes(a->dtype),
+                               {{"target", target}, {"image_grad", image_grad}, {"loss", loss}});
+  if (ra) return ra;
   const int cb = a->emission_channels ? a->emission_channels : int(a->input_shape[4]);
   if (loss_channels <= 0 || loss_channels > cb)
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2: loss_channels must be in 1..%d", cb);
@@ -1182,6 +1193,9 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   if (a->accumulate && a->grad_mode != NGT_GRAD_EXACT)
     return fail(NGT_ERR_UNSUPPORTED, "raymarch_bwd: accumulate needs the exact gradient");
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: the forward output is required");
+  if ((rc = check_aligned("raymarch_bwd", arith_bytes(a->fwd.dtype),
+                          {{"output", a->output}, {"output_grad", a->output_grad}, {"input_grad", a->input_grad}})))
+    return rc;
   if ((rc = check_prepared_quad(&a->fwd))) return rc;
   const Layout l = bwd_layout(a);
   if (!a->workspace || a->workspace_bytes < l.total)
@@ -1332,6 +1346,8 @@ int make_batch(const ngt_raymarch_args* const* items, int count, char* ws, size_
       order[j - 1] = t;
     }
   if (!ws) return fail(NGT_ERR_WORKSPACE, "raymarch batch: null workspace");
+  const int ra = check_aligned("raymarch batch", kScratchAlign, {{"workspace", ws}});
+  if (ra) return ra;
   const size_t need = batch_bytes(items, count);
   if (ws_bytes < need) return fail(NGT_ERR_WORKSPACE, "raymarch batch: needs %zu workspace bytes", need);
   bp = RayBatch{};
@@ -1462,6 +1478,9 @@ int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32
   for (int i = 0; i < count; ++i) {
     const ngt_raymarch_grad_args& g = items[i];
     if (!g.output || !g.output_grad || !g.input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null pointer");
+    const int ra = check_aligned("raymarch batch", arith_bytes(g.fwd.dtype),
+                                 {{"output", g.output}, {"output_grad", g.output_grad}, {"input_grad", g.input_grad}});
+    if (ra) return ra;
     if (g.fwd.quad) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: builds its own quad layouts");
     if (g.grad_mode != NGT_GRAD_EXACT || g.fwd.blending_mode != NGT_BEER_LAMBERT || g.fwd.interpolation != NGT_LINEAR ||
         g.accumulate)

@@ -153,7 +153,7 @@ int validate(const ngt_reduce_blend_args* a) {
   if (!(a->blending_mode == NGT_BEER_LAMBERT || a->blending_mode == NGT_ALPHA ||
         a->blending_mode == NGT_ALPHA_ADDITIVE || a->blending_mode == NGT_ADDITIVE))
     return fail(NGT_ERR_INVALID_ARGUMENT, "Unkown blend_mode");
-  return NGT_OK;
+  return check_aligned("reduce_blend", arith_bytes(a->dtype), {{"input", a->input}, {"output", a->output}});
 }
 
 template <int C, class S>
@@ -212,6 +212,9 @@ extern "C" int ngt_reduce_blend_bwd(const ngt_reduce_blend_grad_args* g, void* s
   int rc = validate(&g->fwd);
   if (rc) return rc;
   if (!g->output_grad || !g->input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "reduce_blend_bwd: null pointer");
+  if ((rc = check_aligned("reduce_blend_bwd", arith_bytes(g->fwd.dtype),
+                          {{"output", g->output}, {"output_grad", g->output_grad}, {"input_grad", g->input_grad}})))
+    return rc;
   if (g->grad_mode == NGT_GRAD_REFERENCE && !g->output)
     return fail(NGT_ERR_INVALID_ARGUMENT, "reduce_blend_bwd: reference mode needs the forward output");
   if (g->grad_mode != NGT_GRAD_EXACT && g->grad_mode != NGT_GRAD_REFERENCE)

@@ -485,7 +485,10 @@ int validate_lut(const ngt_sample_lut_args* a) {
   if (a->normalized_coords && a->cell_center_offset != 0.5f)
     return fail(NGT_ERR_INVALID_ARGUMENT, "Invalid cell center offset must be 0.5 when using normalized coordinates.");
   if (!a->input || !a->lookup) return fail(NGT_ERR_INVALID_ARGUMENT, "sample_lut: null pointer");
-  return NGT_OK;
+  if ((rc = check_aligned("sample_lut", elem_size(a->dtype),
+                          {{"input", a->input}, {"lookup", a->lookup}, {"output", a->output}})))
+    return rc;
+  return check_aligned("sample_lut", kScratchAlign, {{"workspace", a->workspace}});
 }
 
 template <class T>
@@ -604,7 +607,11 @@ int validate_xf(const ngt_sample_transform_args* a) {
     return fail(NGT_ERR_INVALID_ARGUMENT, "sample_transform: num_mipmaps out of range for the grid size");
   if (!a->input || !a->matrix_m || !a->matrix_v || !a->matrix_p || !a->frustum)
     return fail(NGT_ERR_INVALID_ARGUMENT, "sample_transform: null pointer");
-  return NGT_OK;
+  if ((rc = check_aligned("sample_transform", elem_size(a->dtype), {{"input", a->input}, {"output", a->output}})) ||
+      (rc = check_aligned("sample_transform", sizeof(float), {{"matrix_m", a->matrix_m}, {"matrix_v", a->matrix_v},
+                                                              {"matrix_p", a->matrix_p}, {"frustum", a->frustum}})))
+    return rc;
+  return check_aligned("sample_transform", kScratchAlign, {{"workspace", a->workspace}});
 }
 
 template <class T>
@@ -699,6 +706,10 @@ extern "C" int ngt_mip_build(int32_t dtype, const int64_t input_shape[5], const 
   int rc = validate_grid(input_shape, "mip_build");
   if (rc) return rc;
   if (!mip_levels_ok(input_shape, levels)) return fail(NGT_ERR_INVALID_ARGUMENT, "mip_build: levels out of range");
+  if ((dtype == NGT_F32 || dtype == NGT_F64) &&
+      ((rc = check_aligned("mip_build", elem_size(dtype), {{"input", input}})) ||
+       (rc = check_aligned("mip_build", kScratchAlign, {{"pyramid", pyramid}}))))
+    return rc;
   if (dtype == NGT_F32) {
     Mips<float> m;
     return build_mips<float>(input_shape, static_cast<const float*>(input), levels, pyramid, pyramid_bytes,
@@ -739,6 +750,11 @@ extern "C" int ngt_sample_lut_bwd(const ngt_sample_lut_grad_args* a, void* strea
   if (rc) return rc;
   if (a->fwd.mipmapping != NGT_MIP_NONE) return fail(NGT_ERR_UNSUPPORTED, "gradients of mipmapped sampling are not supported");
   if (!a->output_grad || !a->input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "sample_lut_bwd: null pointer");
+  if ((rc = check_aligned("sample_lut_bwd", elem_size(a->fwd.dtype),
+                          {{"output_grad", a->output_grad}, {"input_grad", a->input_grad},
+                           {"lookup_grad", a->lookup_grad}})) ||
+      (rc = check_aligned("sample_lut_bwd", kScratchAlign, {{"workspace", a->workspace}})))
+    return rc;
   if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "sample_lut_bwd: invalid grad_mode");
   if (a->deterministic && a->grad_mode == NGT_GRAD_EXACT && a->fwd.interpolation != NGT_LINEAR)
@@ -772,6 +788,10 @@ extern "C" int ngt_sample_transform_bwd(const ngt_sample_transform_grad_args* a,
   if (rc) return rc;
   if (a->fwd.mipmapping != NGT_MIP_NONE) return fail(NGT_ERR_UNSUPPORTED, "gradients of mipmapped sampling are not supported");
   if (!a->output_grad || !a->input_grad) return fail(NGT_ERR_INVALID_ARGUMENT, "sample_transform_bwd: null pointer");
+  if ((rc = check_aligned("sample_transform_bwd", elem_size(a->fwd.dtype),
+                          {{"output_grad", a->output_grad}, {"input_grad", a->input_grad}})) ||
+      (rc = check_aligned("sample_transform_bwd", kScratchAlign, {{"workspace", a->workspace}})))
+    return rc;
   if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "sample_transform_bwd: invalid grad_mode");
   if (a->fwd.dtype == NGT_F64) return xf_bwd_typed<double>(a, as_stream(stream));
@@ -783,6 +803,9 @@ extern "C" int ngt_lod_transform(const ngt_lod_args* a, void* stream) {
     return fail(NGT_ERR_INVALID_ARGUMENT, "lod_transform: null pointer");
   if (!positive_shape(a->input_dhw, 3) || !positive_shape(a->output_dhw, 3) || a->num_cameras <= 0)
     return fail(NGT_ERR_INVALID_ARGUMENT, "lod_transform: shapes must be positive");
+  const int ra = check_aligned("lod_transform", sizeof(float), {{"matrix_mv", a->matrix_mv}, {"matrix_p", a->matrix_p},
+                                                                {"frustum", a->frustum}, {"output", a->output}});
+  if (ra) return ra;
   int cm;
   if (a->linearize_depth) cm = a->inverse_transform ? NGT_TRANSFORM_LINDEPTH_REVERSE : NGT_TRANSFORM_LINDEPTH;
   else cm = a->inverse_transform ? NGT_TRANSFORM_REVERSE : NGT_TRANSFORM;

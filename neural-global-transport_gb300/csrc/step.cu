@@ -45,6 +45,11 @@ extern "C" int ngt_image_l2_loss(int32_t dtype, int64_t pixels, int32_t channels
   if (!image || !target || !image_grad || !loss) return fail(NGT_ERR_INVALID_ARGUMENT, "image_l2_loss: null pointer");
   if (pixels <= 0 || channels <= 0 || loss_channels <= 0 || loss_channels > channels)
     return fail(NGT_ERR_INVALID_ARGUMENT, "image_l2_loss: invalid sizes");
+  if (dtype == NGT_F32 || dtype == NGT_F64) {
+    const int rc = check_aligned("image_l2_loss", arith_bytes(dtype), {{"image", image}, {"target", target},
+                                                                       {"image_grad", image_grad}, {"loss", loss}});
+    if (rc) return rc;
+  }
   const unsigned nb = ceil_div_u(pixels, kBlock);
   if (dtype == NGT_F64)
     k_l2<double><<<nb, kBlock, 0, as_stream(stream)>>>(pixels, channels, loss_channels, (const double*)image,

@@ -261,3 +261,76 @@ def test_struct_layouts_match_the_header(lib):
     for name, cls in mirrors.items():
         assert lib.ngt_struct_size(name.encode()) == ctypes.sizeof(cls), name
     assert lib.ngt_struct_size(b"ngt_no_such_args") == 0
+
+
+def test_misaligned_buffers_rejected(lib):
+    """A device buffer that does not start on a multiple of its element size (a
+    workspace, camera block or prepared quad layout: of 16 / 256 bytes) is
+    rejected with a status code naming it, before any device work."""
+    from ngt_gb300 import _lib as L
+    a = L.AdvectArgs()
+    a.dtype, a.grid_dhw, a.channels = L.F32, L.I64x3(4, 4, 4), 1
+    for f in ("data", "vel_x", "vel_y", "vel_z", "output", "fwd_field"):
+        setattr(a, f, ctypes.c_void_p(0x1000))
+    a.order, a.clamp, a.boundary = 2, 1, 1
+    for f, addr in (("data", 0x1002), ("lookup", 0x1001), ("extrema", 0x1006)):
+        old = getattr(a, f)
+        setattr(a, f, ctypes.c_void_p(addr))
+        assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+        assert f.encode() in lib.ngt_last_error_message() and b"aligned" in lib.ngt_last_error_message()
+        setattr(a, f, old)
+    a.dtype = L.BF16  # 16-bit storage: two-byte data, float scratch
+    a.data = ctypes.c_void_p(0x1002)
+    a.fwd_field = ctypes.c_void_p(0x1002)
+    assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"fwd_field" in lib.ngt_last_error_message()
+    a.dtype, a.data, a.fwd_field = L.F32, ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000)
+    g = L.AdvectGradArgs()
+    g.fwd = a
+    g.output_grad = g.data_grad = ctypes.c_void_p(0x1000)
+    g.workspace, g.workspace_bytes = ctypes.c_void_p(0x1008), 1 << 20
+    assert lib.ngt_advect_maccormack_bwd(ctypes.byref(g), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"workspace" in lib.ngt_last_error_message()
+
+    v = L.AdvectVelocityArgs()
+    v.dtype, v.grid_dhw, v.order, v.clamp, v.boundary = L.F32, L.I64x3(4, 4, 4), 1, 0, 1
+    for f in ("vel_x", "vel_y", "vel_z", "out_x", "out_y", "out_z"):
+        setattr(v, f, ctypes.c_void_p(0x1000))
+    v.lookup[1] = 0x1003
+    assert lib.ngt_advect_velocity_fwd(ctypes.byref(v), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"lookup[1]" in lib.ngt_last_error_message()
+
+    r = L.RaymarchArgs()
+    r.dtype = L.F32
+    r.input_shape = L.I64x5(1, 6, 5, 4, 1)
+    r.output_dhw = L.I64x3(4, 4, 4)
+    for f in ("input", "output", "matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(r, f, ctypes.c_void_p(0x1000))
+    r.num_cameras = 1
+    r.interpolation, r.boundary, r.blending_mode, r.separate_camera_batch = 1, 0, 0, 1
+    for f, addr in (("input", 0x1001), ("matrix_v", 0x1002), ("cameras", 0x1004), ("quad", 0x1010),
+                    ("workspace", 0x1008)):
+        old = getattr(r, f)
+        setattr(r, f, ctypes.c_void_p(addr))
+        assert lib.ngt_raymarch_fwd(ctypes.byref(r), None) == L.NGT_ERR_INVALID_ARGUMENT
+        assert f.encode() in lib.ngt_last_error_message()
+        setattr(r, f, old)
+    assert lib.ngt_raymarch_fwd_l2(ctypes.byref(r), ctypes.c_void_p(0x1000), 1, ctypes.c_void_p(0x1002),
+                                   ctypes.c_void_p(0x1000), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"image_grad" in lib.ngt_last_error_message()
+    rg = L.RaymarchGradArgs()
+    rg.fwd = r
+    rg.output, rg.output_grad, rg.input_grad = ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1001)
+    assert lib.ngt_raymarch_bwd(ctypes.byref(rg), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"input_grad" in lib.ngt_last_error_message()
+
+    s = L.SampleLutArgs()
+    s.dtype = L.F32
+    s.input_shape, s.lookup_shape = L.I64x5(1, 4, 4, 4, 1), L.I64x5(1, 2, 2, 2, 4)
+    s.input, s.lookup, s.output = ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1002), ctypes.c_void_p(0x1000)
+    s.interpolation, s.boundary, s.separate_camera_batch, s.relative_coords = 1, 0, 1, 1
+    assert lib.ngt_sample_lut_fwd(ctypes.byref(s), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"lookup" in lib.ngt_last_error_message()
+    assert lib.ngt_image_l2_loss(L.F32, 4, 2, 1, ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1001),
+                                 ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"target" in lib.ngt_last_error_message()
