@@ -4,6 +4,8 @@ Each ``csrc/*.cu`` file is compiled by nvcc in parallel into an object, then
 the objects are linked into a shared library next to this file.  The CUDA
 runtime is linked statically, so the library needs only the driver.
 Rebuilds are skipped when no source or header is newer than the library.
+ptxas's resource report of every kernel (registers, spills, shared memory) is
+kept beside each object as ``_build/<source>.ptxas.txt``.
 """
 import concurrent.futures
 import glob
@@ -19,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libngt_ops.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xptxas", "-warn-spills", "-I", INCLUDE, "-I", CSRC]
+         "-Xptxas", "-warn-spills", "-Xptxas", "-v", "-I", INCLUDE, "-I", CSRC]
 
 
 def nvcc():
@@ -41,6 +43,11 @@ def _deps():
     return _sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h")) + [__file__]
 
 
+def resource_report(src):
+    """Path of ptxas's resource report for source ``src`` (written by the build)."""
+    return os.path.join(BUILD, os.path.basename(src) + ".ptxas.txt")
+
+
 def up_to_date():
     if not os.path.exists(LIB):
         return False
@@ -60,8 +67,12 @@ def build_library(force=False, verbose=False, extra_flags=()):
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s" % (src, res.stderr[-8000:]))
-        if verbose and res.stderr.strip():
-            print(res.stderr)
+        with open(resource_report(src), "w") as f:
+            f.write(res.stderr)
+        if verbose:
+            warnings = [l for l in res.stderr.splitlines() if "ptxas info" not in l]
+            if warnings:
+                print("\n".join(warnings))
         return obj
 
     srcs = _sources()

@@ -1,0 +1,76 @@
+"""Register budgets of the step's kernels, read from ptxas's resource report of
+the in-tree build (no GPU needed).
+
+The kernels are sized for residency: the render forward and one-pass backward at
+48 registers (10 blocks of 128 threads per SM); MacCormack forward 1 at 32
+(8 blocks of 256) and backward 2 at 48 (5 blocks of 256), the same for 16-bit
+storage as for f32.  One register more costs a resident block per SM, so a
+change that crosses a budget fails here rather than only in a timing run.
+"""
+import os
+import re
+
+import pytest
+
+import __graft_entry__
+
+
+@pytest.fixture(scope="module")
+def reports():
+    __graft_entry__.load_package()
+    from ngt_gb300 import _build
+    srcs = [os.path.join(_build.CSRC, n) for n in ("advect.cu", "raymarch.cu")]
+    if not all(os.path.exists(_build.resource_report(s)) for s in srcs):
+        _build.build_library(force=True)
+    out = {}
+    for s in srcs:
+        out.update(parse(open(_build.resource_report(s)).read()))
+    return out
+
+
+def parse(text):
+    """{mangled kernel name: (registers, spill store bytes, spill load bytes)}"""
+    res, cur, spill = {}, None, (0, 0)
+    for line in text.splitlines():
+        m = re.search(r"Compiling entry function '([^']+)'", line)
+        if m:
+            cur, spill = m.group(1), (0, 0)
+            continue
+        m = re.search(r"(\d+) bytes spill stores, (\d+) bytes spill loads", line)
+        if m and cur:
+            spill = (int(m.group(1)), int(m.group(2)))
+        m = re.search(r"Used (\d+) registers", line)
+        if m and cur:
+            res[cur] = (int(m.group(1)),) + spill
+            cur = None
+    return res
+
+
+def find(reports, *parts):
+    hits = [v for k, v in reports.items() if all(p in k for p in parts)]
+    assert len(hits) == 1, (parts, len(hits))
+    return hits[0]
+
+
+STORAGE = {"f32": "f", "bf16": "13__nv_bfloat16", "f16": "6__half"}
+
+
+@pytest.mark.parametrize("storage", sorted(STORAGE))
+def test_maccormack_register_budgets(reports, storage):
+    t = STORAGE[storage]
+    regs, st, ld = find(reports, "k_mc_fwd1ILi1E" + t + "NS0_14CenteredLookup")
+    assert regs <= 32 and st == ld == 0
+    regs, st, ld = find(reports, "k_mc_bwd2ILi1E" + t + "NS0_12StoredLookup")
+    assert regs <= 48 and st == ld == 0
+
+
+@pytest.mark.parametrize("kernel", ["k_raymarch_fwdILi1ELi2EffE", "k_raymarch_bwd_blILi1ELi2EffE"])
+def test_render_register_budgets(reports, kernel):
+    regs, st, ld = find(reports, kernel)
+    assert regs <= 48 and st == ld == 0
+
+
+def test_quad_kernels_do_not_spill(reports):
+    for k in ("k_quad_foldEPK6float4", "k_quad_buildIfEE"):
+        _, st, ld = find(reports, k)
+        assert st == ld == 0
