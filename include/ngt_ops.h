@@ -265,9 +265,11 @@ size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* args);
  * the scratch is a 16 MiB static device array that every GPU using the library
  * holds until exit, shared by all calls and keeping the last call's contents
  * (each call clears what must start at zero).  Calls needing more (see
- * ngt_raymarch_bwd_workspace_bytes) fail with NGT_ERR_WORKSPACE.  The first call
- * on a device looks up the array's device address: make it before any stream
- * capture.  Calls whose GPU work overlaps race on the array. */
+ * ngt_raymarch_bwd_workspace_bytes) fail with NGT_ERR_WORKSPACE.  Each call made
+ * outside a stream capture looks up the array's device address in the current
+ * context; a call under capture reuses the last address found on its device, so
+ * the first call on a device (and the first after a device reset) must come
+ * before any stream capture.  Calls whose GPU work overlaps race on the array. */
 int ngt_raymarch_bwd_static(const ngt_raymarch_grad_args* args, void* stream);
 
 /* ------------------------------------------------------------ reduce blend */

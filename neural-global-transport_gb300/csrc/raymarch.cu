@@ -1549,9 +1549,13 @@ extern "C" int ngt_raymarch_bwd_batch_after_fwd(const ngt_raymarch_grad_args* it
 // the reference-mode buffers) is cleared inside each call by ngt_raymarch_bwd's
 // own stream-ordered memsets.  Calls whose work overlaps on the GPU (other
 // streams, other host threads) race on the array.  In host code the array's
-// name is only a stand-in: its device address is looked up with
-// cudaGetSymbolAddress by the first call on each device, with that device
-// current, and that first call should come before any stream capture.
+// name is only a stand-in: its device address in the calling thread's current
+// context is looked up with cudaGetSymbolAddress by every call made outside a
+// stream capture (so a device reset or another context of the same device
+// gets its own address); a call made while its stream is being captured uses
+// the address the last uncaptured call on that device found, so the first
+// call on a device (and the first after a device reset) comes before any
+// capture.
 constexpr size_t kStaticScratchBytes = size_t(16) << 20;
 static __device__ __align__(256) unsigned char g_raymarch_scratch[kStaticScratchBytes];
 
@@ -1563,18 +1567,24 @@ constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void* g_scratch_ptr[kMaxDevices] = {};
 
-// The array's device address on the current device, looked up once per device.
-int scratch_address(void** out) {
+// The array's device address on the current device: looked up afresh outside
+// stream capture, the last looked-up address during a capture of ``st``.
+int scratch_address(cudaStream_t st, void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("raymarch_bwd_static: cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return fail(NGT_ERR_UNSUPPORTED, "raymarch_bwd_static: device %d", dev);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return check_launch("raymarch_bwd_static: cudaStreamIsCapturing");
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_raymarch_scratch);
     if (e != cudaSuccess)
       return fail(NGT_ERR_CUDA, "raymarch_bwd_static: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
     g_scratch_ptr[dev] = p;
+  } else if (!g_scratch_ptr[dev]) {
+    return fail(NGT_ERR_UNSUPPORTED,
+                "raymarch_bwd_static: the first call on device %d must come before any stream capture", dev);
   }
   *out = g_scratch_ptr[dev];
   return NGT_OK;
@@ -1585,12 +1595,18 @@ int scratch_address(void** out) {
 
 extern "C" int ngt_raymarch_bwd_static(const ngt_raymarch_grad_args* a, void* stream) {
   if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd_static: null arguments");
+  int cin, cb;
+  // the same argument checks as ngt_raymarch_bwd before the scratch size is formed from the shapes
+  int rc = validate(&a->fwd, cin, cb);
+  if (rc) return rc;
+  if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: invalid grad_mode");
   const size_t need = bwd_layout(a).total;
   if (need > kStaticScratchBytes)
     return fail(NGT_ERR_WORKSPACE, "raymarch_bwd_static: this call needs %zu scratch bytes, above the %zu-byte static scratch",
                 need, kStaticScratchBytes);
   void* scratch = nullptr;
-  const int rc = scratch_address(&scratch);
+  rc = scratch_address(as_stream(stream), &scratch);
   if (rc) return rc;
   ngt_raymarch_grad_args b = *a;
   b.workspace = scratch;

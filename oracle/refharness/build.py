@@ -17,7 +17,8 @@ shared libraries in ``oracle/_ref/``.  The reference tree must be present
 (it is only in the development container, never on the GPU host), so this
 runs where the golden vectors are generated.
 
-Usage: ``python oracle/refharness/build.py [--ref /path/to/reference]``
+Usage: ``python oracle/refharness/build.py [--ref /path/to/reference]`` (default: the
+``NGT_REFERENCE_ROOT`` environment variable, else the development container's tree)
 """
 import argparse
 import os
@@ -26,7 +27,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-DEFAULT_REF = "/root/reference"
+# where the reference tree lies in the development container (this recipe reads
+# the reference's sources from there); NGT_REFERENCE_ROOT or --ref point elsewhere
+DEFAULT_REF = os.environ.get("NGT_REFERENCE_ROOT", "/root/reference")
 SRC = "phitest/render/cuda/src"
 
 # (head, [(file, first_line, last_line)], driver, output)

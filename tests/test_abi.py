@@ -108,6 +108,28 @@ def test_raymarch_validation(lib):
     assert lib.ngt_raymarch_bwd(ctypes.byref(g), None) == L.NGT_ERR_UNSUPPORTED
 
 
+def test_static_scratch_backward_validates_before_sizing(lib):
+    """The static-scratch backward checks the arguments as ngt_raymarch_bwd does
+    before it forms its scratch size from the shapes: a negative or absurd shape
+    is an invalid argument, not a scratch-size failure."""
+    from ngt_gb300 import _lib as L
+    g = L.RaymarchGradArgs()
+    r = g.fwd
+    r.dtype = L.F32
+    r.output_dhw = L.I64x3(4, 4, 4)
+    for f in ("input", "output", "matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(r, f, ctypes.c_void_p(0x1000))
+    r.num_cameras = 1
+    r.interpolation, r.boundary, r.blending_mode, r.separate_camera_batch = 1, 0, 0, 1
+    g.output = g.output_grad = g.input_grad = ctypes.c_void_p(0x1000)
+    for shape in ((1, -4, 4, 4, 1), (1, 1 << 40, 1 << 40, 4, 1), (1, 4, 4, 4, 3)):
+        g.fwd.input_shape = L.I64x5(*shape)
+        assert lib.ngt_raymarch_bwd_static(ctypes.byref(g), None) == L.NGT_ERR_INVALID_ARGUMENT, shape
+    g.fwd.input_shape = L.I64x5(1, 4, 4, 4, 1)
+    g.grad_mode = 9
+    assert lib.ngt_raymarch_bwd_static(ctypes.byref(g), None) == L.NGT_ERR_INVALID_ARGUMENT
+
+
 def test_advect_validation(lib):
     from ngt_gb300 import _lib as L
     a = L.AdvectArgs()

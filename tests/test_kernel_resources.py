@@ -20,6 +20,7 @@ def reports():
     __graft_entry__.load_package()
     from ngt_gb300 import _build
     srcs = [os.path.join(_build.CSRC, n) for n in ("advect.cu", "raymarch.cu")]
+    _build.build_library()  # rebuilds (and rewrites the reports) when a source is newer than the library
     if not all(os.path.exists(_build.resource_report(s)) for s in srcs):
         _build.build_library(force=True)
     out = {}
