@@ -178,135 +178,80 @@ def measured_peak_hbm():
 
 
 # ------------------------------------------------------------------- CPU legs
-_CPU_INPUTS = {}  # per process: inputs of the CPU samples, generated once
+# The CPU implementation of the step is the oracle, the NumPy restatement of the
+# reference's operators (the reference itself has no CPU path: REGISTER__CPU is
+# empty, resample_grid.cc:1179-1181, and its CUDA build needs TensorFlow 1.12).
+# Every CPU step below is one FULL step of the headline workload -- 128^3
+# MacCormack warp, 5 views of 256 x 256 x 128, image L2, backward to density and
+# velocity -- split over spawned host processes by oracle.parallel (warp as
+# z-slabs with halos, render as bands of image rows): nothing is sampled or
+# scaled.
+CPU_SAMPLE = ("one full step (128^3 MacCormack warp + 5-view 256x256x128 render + L2 + backward) of the oracle, "
+              "the NumPy restatement of the reference operators (the reference has no CPU path), split over %d "
+              "spawned host processes: warp and its adjoint as z-slabs with halos, render as 8-row image bands")
 
 
-def _cpu_inputs(key, make):
-    if key not in _CPU_INPUTS:
-        _CPU_INPUTS[key] = make()
-    return _CPU_INPUTS[key]
-
-
-def _cpu_adv_task(n):
-    """Advection forward + backward of the oracle on an n^3 grid."""
-    sys.path.insert(0, ROOT)
-    import __graft_entry__
-    __graft_entry__.load_package()
-    from ngt_gb300 import synthetic
-    from oracle import advect
-    rho, ux, uy, uz = _cpu_inputs(("adv", n), lambda: (synthetic.gaussian_blobs((n, n, n), seed=0),)
-                                  + tuple(synthetic.curl_noise_mac((n, n, n), max_u=2.0, seed=1)))
-    t0 = time.perf_counter()
-    out = advect.density_maccormack(rho, ux, uy, uz)
-    advect.density_maccormack_grad(rho, ux, uy, uz, out)
-    return time.perf_counter() - t0
-
-
-def _cpu_render_task(view, rows):
-    """Render forward + exact backward of ``rows`` image rows of one view, oracle."""
-    sys.path.insert(0, ROOT)
+def cpu_inputs():
+    """The headline workload's inputs and its targets (rendered by the oracle)."""
     import __graft_entry__
     __graft_entry__.load_package()
     from ngt_gb300 import workloads
-    from oracle import ops
-    w = _cpu_inputs("config2", workloads.config2)
-    D, H, W = w.image_dhw
-    # a band of rows through the image centre: same per-ray work as the full view
-    P = w.P[view:view + 1].copy()
-    Pm = P.reshape(4, 4).T.copy()
-    Pm[1, 1] *= H / rows  # narrow the frustum vertically to the band
-    P[0] = Pm.T.reshape(16)
-    F = w.F[view:view + 1].copy()
-    F[0, 4] *= rows / H
-    F[0, 5] *= rows / H
-    scale = np.asarray([w.depth_step, w.depth_step], np.float32)
-    x = (w.rho * scale).astype(np.float32)[None]
+    return workloads.config2()
+
+
+def cpu_step(pool, nproc, w, targets):
+    """Seconds of one full differentiated step of the oracle on the host."""
+    from oracle import parallel
     t0 = time.perf_counter()
-    y = ops.raymarch_grid_transform(x, w.M, w.V[view:view + 1], P, F, [D, rows, W])
-    g = np.zeros_like(y)
-    g[..., 0] = y[..., 0]
-    ops.raymarch_grid_transform_grad(x, y, g, w.M, w.V[view:view + 1], P, F, [D, rows, W])
+    parallel.render_advect_step(pool, nproc, w.rho, w.ux, w.uy, w.uz, w.M, w.V, w.P, w.F, targets, w.image_dhw,
+                                w.depth_step)
     return time.perf_counter() - t0
 
 
-def cpu_step_time(processes, adv_n=64, rows=8, pool=None):
-    """Estimated seconds of one full step on the host: the advection timed on an
-    adv_n^3 grid and the render on ``rows`` rows of every view, each scaled
-    linearly by its share of the full work; with processes > 1 the render bands
-    run in parallel worker processes (spawned, no CUDA in them; ``pool``: such a
-    pool kept across calls)."""
-    import multiprocessing as mp
-    full = 128 ** 3
-    t_adv = _cpu_adv_task(adv_n) * (full / adv_n ** 3)
-    views = 5
-    if processes > 1:
-        own = pool is None
-        if own:
-            pool = mp.get_context("spawn").Pool(min(processes, views))
-        try:
-            t0 = time.perf_counter()
-            pool.starmap(_cpu_render_task, [(v, rows) for v in range(views)])
-            t_render_wall = time.perf_counter() - t0
-        finally:
-            if own:
-                pool.close()
-                pool.join()
-        # rows of a view are independent: with P processes the full render takes
-        # (256/rows) * views bands / P band-times
-        per_band = t_render_wall / ((views + min(processes, views) - 1) // min(processes, views))
-        t_render = per_band * (256 / rows) * views / processes
-    else:
-        t_render = sum(_cpu_render_task(v, rows) for v in range(views)) * (256 / rows)
-    return t_adv + t_render, {"advect_sample": "%d^3 grid, scaled x%.0f" % (adv_n, full / adv_n ** 3),
-                              "render_sample": "%d of 256 rows per view, 5 views, scaled x%d" % (rows, 256 // rows)}
+# Wall-clock budget of the reference arm's timed steps (seconds): a run asking for
+# more steps than fit stops there and reports ``steps_timed``.
+REFERENCE_BUDGET_S = 240.0
 
 
-# Wall-clock budget of the reference arm's timed steps (seconds): the per-step
-# sample shrinks with the step count and timing stops once the budget is spent.
-REFERENCE_BUDGET_S = 150.0
-
-
-def reference_sample_plan(calls):
-    """(advection grid side, image rows per view) of each reference step's
-    sample for a run of ``calls`` steps (warm-up included); smaller samples than
-    32^3 and 2 rows are dominated by NumPy call overhead and overstate the
-    scaled step time, so long runs stop at the budget instead."""
-    return (48, 4) if calls <= 10 else (32, 2)
+def reference_setup():
+    """(pool, processes, workload, targets) of the reference arm: a pool of spawned
+    workers over every host CPU and the targets rendered by the oracle (untimed)."""
+    from oracle import parallel
+    w = cpu_inputs()
+    pool, nproc = parallel.make_pool()
+    try:
+        tgt, _, _ = parallel.render_l2(pool, nproc, w.rho_target, w.depth_step, w.M, w.V, w.P, w.F, w.image_dhw)
+    except BaseException:
+        pool.close()
+        raise
+    return pool, nproc, w, np.ascontiguousarray(tgt[..., :1])
 
 
 def reference_arm(args, world, rank):
     if rank != 0:
         return
-    import multiprocessing as mp
-    procs = os.cpu_count() or 1
-    adv_n, rows = reference_sample_plan(args.warmup + args.steps)
+    pool, nproc, w, tgt = reference_setup()
     times = []
-    # one worker pool for all steps (a single step makes its own)
-    pool = mp.get_context("spawn").Pool(min(procs, 5)) if procs > 1 and args.warmup + args.steps > 1 else None
     try:
+        for _ in range(args.warmup):
+            cpu_step(pool, nproc, w, tgt)
         t_begin = time.perf_counter()
-        for i in range(args.warmup + args.steps):
-            if i == args.warmup:
-                t_begin = time.perf_counter()
-            t, sample = cpu_step_time(procs, adv_n=adv_n, rows=rows, pool=pool)
-            if i >= args.warmup:
-                times.append(t)
-                if time.perf_counter() - t_begin > REFERENCE_BUDGET_S:
-                    break
+        for _ in range(args.steps):
+            times.append(cpu_step(pool, nproc, w, tgt))
+            if time.perf_counter() - t_begin > REFERENCE_BUDGET_S:
+                break
     finally:
-        if pool is not None:
-            pool.close()
-            pool.join()
+        pool.close()
+        pool.join()
     value = 1.0 / float(np.mean(times))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "steps_timed": len(times), "warmup": args.warmup, "ms_per_step": 1e3 / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": [128, 128, 128], "views": 5, "image": [256, 256],
                        "depth_samples": 128},
-            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": procs, "kind": "port",
-                             "sample": "NumPy restatement of the reference operators (the reference has no CPU "
-                                       "path); per step: %s; %s" % (sample["advect_sample"], sample["render_sample"]),
-                             "host": host_cpu()},
+            "timed_s": float(np.sum(times)),
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": nproc, "kind": "port",
+                             "sample": CPU_SAMPLE % nproc, "host": host_cpu()},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -401,10 +346,15 @@ def gpu_arm(args, world, rank, local):
     if e2e_step:
         line["e2e_step"] = e2e_step
     if rank == 0 and world == 1 and args.cpu_baseline == "on":
-        t, sample = cpu_step_time(1, adv_n=48, rows=4)
-        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": 1, "kind": "port",
-                                "sample": "oracle (NumPy fp32, single process) per step: %s; %s"
-                                          % (sample["advect_sample"], sample["render_sample"]),
+        from oracle import parallel
+        pool, nproc = parallel.make_pool()  # spawned workers: no CUDA in them
+        try:
+            t = cpu_step(pool, nproc, w, np.ascontiguousarray(tgt.cpu().numpy()))
+        finally:
+            pool.close()
+            pool.join()
+        line["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": nproc, "kind": "port",
+                                "sample": CPU_SAMPLE % nproc + "; the same inputs and targets as the GPU step",
                                 "host": host_cpu()}
     if rank == 0:
         print(json.dumps(line), flush=True)

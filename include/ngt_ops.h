@@ -459,6 +459,33 @@ int ngt_image_l2_loss(int32_t dtype, int64_t pixels, int32_t channels, int32_t l
 int ngt_raymarch_fwd_l2(const ngt_raymarch_args* args, const void* target, int32_t loss_channels, void* image_grad,
                         void* loss, void* stream);
 
+/* Background composite of the render composition, replacing the TensorFlow
+ * ops of Renderer.render_density (renderer.py:779-781, 804-806): with t =
+ * exp(-d) the transmittance of each ray (d the image's last, optical-depth
+ * channel) the camera's background shows through behind the light channels,
+ * output_c = image_c + background_c * t, and the depth channel is cut
+ * (cut_alpha).  image: batch x pixels x C (C in {2, 4}; pixels = V * H * W);
+ * background: pixels x (C - 1), shared by the batch entries; output: batch x
+ * pixels x (C - 1).  F32 or F64.  The backward writes image_grad (the light
+ * channels' gradient, and -t * sum_c background_c * g_c in the depth channel)
+ * and, if background_grad is not null, the background's gradient (summed over
+ * the batch). */
+int ngt_background_composite(int32_t dtype, int64_t batch, int64_t pixels, int32_t channels, const void* image,
+                             const void* background, void* output, void* stream);
+int ngt_background_composite_bwd(int32_t dtype, int64_t batch, int64_t pixels, int32_t channels, const void* image,
+                                 const void* background, const void* output_grad, void* image_grad,
+                                 void* background_grad, void* stream);
+/* ngt_raymarch_fwd_l2 with that composite in its epilogue: the loss compares
+ * the composited light channels (background: cameras x H' x W' x (Cb - 1), per
+ * camera, shared by the batch; Beer-Lambert blending) with the target, and
+ * image_grad receives the gradient with respect to the raw output [light, d]
+ * (what ngt_raymarch_bwd takes), the depth channel's being -t * sum_c
+ * background_c * g_c.  The raw render stays in args->output.  loss_channels is
+ * at most Cb - 1.  No reference counterpart as a single call (see
+ * ngt_image_l2_loss). */
+int ngt_raymarch_fwd_l2_background(const ngt_raymarch_args* args, const void* background, const void* target,
+                                   int32_t loss_channels, void* image_grad, void* loss, void* stream);
+
 /* ------------------------------------------------------------ diagnostics */
 const char* ngt_last_error_message(void);
 int ngt_version(void);

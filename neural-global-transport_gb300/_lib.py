@@ -126,6 +126,9 @@ SIGNATURES = {
     "ngt_raymarch_quad_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
     "ngt_raymarch_quad": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp], c_i32),
     "ngt_raymarch_fwd_l2": ([ctypes.POINTER(RaymarchArgs), c_vp, c_i32, c_vp, c_vp, c_vp], c_i32),
+    "ngt_raymarch_fwd_l2_background": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp, c_i32, c_vp, c_vp, c_vp], c_i32),
+    "ngt_background_composite": ([c_i32, c_i64, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp], c_i32),
+    "ngt_background_composite_bwd": ([c_i32, c_i64, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_i32),
     "ngt_raymarch_fwd": ([ctypes.POINTER(RaymarchArgs), c_vp], c_i32),
     "ngt_raymarch_bwd": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
     "ngt_raymarch_bwd_workspace_bytes": ([ctypes.POINTER(RaymarchGradArgs)], c_sz),

@@ -55,6 +55,9 @@ struct RayParams {
   void* l2_grad;
   void* l2_loss;
   int l2_lc;
+  // with the fused loss: per-camera background images (cameras, H, W, CB - 1)
+  // composited behind the light channels before the loss, or null
+  const void* l2_bkg;
 };
 
 // One-channel float / 16-bit grids sampled LINEAR go through the quad layout.
@@ -253,12 +256,35 @@ __device__ __forceinline__ bool tile_pixel(const RayParams& p, int tile, int& px
 }
 
 // Fused image L2 loss of one pixel: the gradient g_c = out_c - target_c on the
-// first l2_lc channels (0 on the others) is written, sum g_c^2 returned.
+// first l2_lc channels (0 on the others) is written, sum g_c^2 returned.  With a
+// background (renderer.py:779, 804-806) the light channels are first composited,
+// out_c + background_c * t with t = exp(-d) the ray's transmittance, and the
+// optical-depth channel receives -t * sum_c background_c * g_c.  ``pix`` is the
+// pixel's index in the output (slot, y, x); its camera's background pixel is
+// formed from it here, after the march, so the loop carries no extra index.
 template <int CB, class S>
 __device__ __forceinline__ S l2_pixel(const RayParams& p, int64_t pix, const S out[CB]) {
   const S* tg = static_cast<const S*>(p.l2_target) + pix * p.l2_lc;
   S* gr = static_cast<S*>(p.l2_grad) + pix * CB;
   S l = S(0);
+  if constexpr (CB > 1) {
+    if (p.l2_bkg) {
+      const int64_t hw = int64_t(p.H) * p.W;
+      const int64_t bq = p.sep ? (pix / hw) % p.ncam * hw + pix % hw : pix;
+      const S* bk = static_cast<const S*>(p.l2_bkg) + bq * (CB - 1);
+      const S t = ex(-out[CB - 1]);
+      S sb = S(0);
+#pragma unroll
+      for (int k = 0; k < CB - 1; ++k) {
+        const S g = k < p.l2_lc ? out[k] + bk[k] * t - tg[k] : S(0);
+        gr[k] = g;
+        l += g * g;
+        sb += bk[k] * g;
+      }
+      gr[CB - 1] = -t * sb;
+      return l;
+    }
+  }
 #pragma unroll
   for (int k = 0; k < CB; ++k) {
     const S g = k < p.l2_lc ? out[k] - tg[k] : S(0);
@@ -1122,7 +1148,7 @@ namespace {
 // through the quad layout; without one every block forms its camera and gathers
 // directly (same results).
 int raymarch_fwd(const ngt_raymarch_args* a, const void* l2_target, int l2_lc, void* l2_grad, void* l2_loss,
-                 void* stream, const char* name) {
+                 const void* l2_bkg, void* stream, const char* name) {
   int cin, cb;
   int rc = validate(a, cin, cb);
   if (rc) return rc;
@@ -1133,6 +1159,7 @@ int raymarch_fwd(const ngt_raymarch_args* a, const void* l2_target, int l2_lc, v
   p.l2_lc = l2_lc;
   p.l2_grad = l2_grad;
   p.l2_loss = l2_loss;
+  p.l2_bkg = l2_bkg;
   cudaStream_t st = as_stream(stream);
   if (a->cameras) p.cams = static_cast<const Cam*>(a->cameras);
   if (a->quad) {
@@ -1160,7 +1187,7 @@ int raymarch_fwd(const ngt_raymarch_args* a, const void* l2_target, int l2_lc, v
 }  // namespace
 
 extern "C" int ngt_raymarch_fwd(const ngt_raymarch_args* a, void* stream) {
-  return raymarch_fwd(a, nullptr, 0, nullptr, nullptr, stream, "ngt_raymarch_fwd");
+  return raymarch_fwd(a, nullptr, 0, nullptr, nullptr, nullptr, stream, "ngt_raymarch_fwd");
 }
 
 extern "C" int ngt_raymarch_fwd_l2(const ngt_raymarch_args* a, const void* target, int32_t loss_channels,
@@ -1173,7 +1200,28 @@ extern "C" int ngt_raymarch_fwd_l2(const ngt_raymarch_args* a, const void* targe
   const int cb = a->emission_channels ? a->emission_channels : int(a->input_shape[4]);
   if (loss_channels <= 0 || loss_channels > cb)
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2: loss_channels must be in 1..%d", cb);
-  return raymarch_fwd(a, target, loss_channels, image_grad, loss, stream, "ngt_raymarch_fwd_l2");
+  return raymarch_fwd(a, target, loss_channels, image_grad, loss, nullptr, stream, "ngt_raymarch_fwd_l2");
+}
+
+extern "C" int ngt_raymarch_fwd_l2_background(const ngt_raymarch_args* a, const void* background, const void* target,
+                                              int32_t loss_channels, void* image_grad, void* loss, void* stream) {
+  if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null arguments");
+  if (!background || !target || !image_grad || !loss)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_background: null pointer");
+  const int ra = check_aligned("raymarch_fwd_l2_background", arith_bytes(a->dtype),
+                               {{"background", background}, {"target", target}, {"image_grad", image_grad},
+                                {"loss", loss}});
+  if (ra) return ra;
+  const int cb = a->emission_channels ? a->emission_channels : int(a->input_shape[4]);
+  if (cb < 2)
+    return fail(NGT_ERR_INVALID_ARGUMENT,
+                "raymarch_fwd_l2_background: the background needs light channels and an optical depth channel");
+  if (a->blending_mode != NGT_BEER_LAMBERT)
+    return fail(NGT_ERR_UNSUPPORTED, "raymarch_fwd_l2_background: the transmittance exp(-d) is Beer-Lambert's");
+  if (loss_channels <= 0 || loss_channels > cb - 1)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_background: loss_channels must be in 1..%d", cb - 1);
+  return raymarch_fwd(a, target, loss_channels, image_grad, loss, background, stream,
+                      "ngt_raymarch_fwd_l2_background");
 }
 
 extern "C" size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* a) {

@@ -657,3 +657,44 @@ def image_l2_loss(image, target, loss_channels=1):
     if not 0 < int(loss_channels) <= C or target.numel() != image.numel() // C * int(loss_channels):
         raise ValueError("image_l2_loss: target must hold loss_channels (1..%d) values per pixel" % C)
     return _ImageL2Loss.apply(image, target, int(loss_channels))
+
+
+# ------------------------------------------------------- background composite
+class _BackgroundComposite(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, image, background):
+        N, V, H, W, C = image.shape
+        out = torch.empty((N, V, H, W, C - 1), dtype=image.dtype, device=image.device)
+        L.call("ngt_background_composite", _code(image), N, V * H * W, C, _ptr(image), _ptr(background), _ptr(out),
+               _stream())
+        ctx.save_for_backward(image, background)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        image, background = ctx.saved_tensors
+        N, V, H, W, C = image.shape
+        gi = torch.empty_like(image)
+        gb = torch.empty_like(background) if ctx.needs_input_grad[1] else None
+        L.call("ngt_background_composite_bwd", _code(image), N, V * H * W, C, _ptr(image), _ptr(background),
+               _ptr(g.contiguous()), _ptr(gi), _ptr(gb), _stream())
+        return gi, gb
+
+
+def background_composite(image, background):
+    """The render composition's background composite (Renderer.render_density,
+    renderer.py:779-781, 804-806): ``image`` (N, V, H, W, C) from a Beer-Lambert
+    raymarch, C in {2, 4} with the optical depth d last; ``background`` the
+    cameras' images behind the volume, broadcast to (V, H, W, C - 1) (one per
+    camera, shared by the batch).  Returns the light channels with the background
+    attenuated by the transmittance, ``image[..., :-1] + background * exp(-d)``
+    (N, V, H, W, C - 1).  Differentiable w.r.t. both."""
+    image = _cuda(image, "image")
+    if image.dtype not in (torch.float32, torch.float64):
+        raise TypeError("background_composite: images are float32 or float64")
+    if image.dim() != 5 or image.shape[-1] not in (2, 4):
+        raise ValueError("background_composite: image is (N, V, H, W, C) with C = 2 or 4")
+    N, V, H, W, C = image.shape
+    background = torch.as_tensor(background, device=image.device).to(image.dtype)
+    background = background.expand(V, H, W, C - 1).contiguous()
+    return _BackgroundComposite.apply(image, background)

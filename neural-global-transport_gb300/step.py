@@ -5,6 +5,7 @@ The step of the density / velocity optimisation (optimization.py:1018-1046 and
 
     rho' = MacCormack(rho, u)                        (warp, MC_SMOOTH, CLAMP)
     image_v = raymarch(rho' as [light*step, step])    (Beer-Lambert, BORDER)
+    (optional) light_v += background_v * exp(-d_v)     (renderer.py:779, 804-806)
     loss = 0.5 * sum_v ||image_v.light - target_v||^2
     backward to rho and to the three MAC face grids
 
@@ -31,7 +32,8 @@ class RenderAdvectStep:
     KERNELS_PER_STEP = 8
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
-                 clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact"):
+                 clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact",
+                 background=None):
         dev = rho.device
         self.lib = L.load()
         self.rho, self.ux, self.uy, self.uz = rho.contiguous(), ux.contiguous(), uy.contiguous(), uz.contiguous()
@@ -60,6 +62,12 @@ class RenderAdvectStep:
         self.g_uz = torch.empty(uz.shape, dtype=f32, device=dev)
         self.loss = torch.zeros((1,), dtype=f32, device=dev)
         self.pixels = nv * hh * ww
+        # the cameras' backgrounds behind the volume (renderer.py:804-806), composited
+        # into the light channel by the loss epilogue: (views, H, W, 1)
+        self.background = None
+        if background is not None:
+            self.background = torch.as_tensor(background, device=dev).to(self.image.dtype).expand(
+                nv, hh, ww, 1).contiguous()
 
         a = L.AdvectArgs()
         a.dtype = _code(rho)
@@ -137,8 +145,12 @@ class RenderAdvectStep:
         self._call("ngt_advect_maccormack_fwd", ctypes.byref(self.adv), s)
         if self.ray_quad is not None:
             self._call("ngt_raymarch_quad", ctypes.byref(self.ray), _ptr(self.ray_quad), s)
-        self._call("ngt_raymarch_fwd_l2", ctypes.byref(self.ray), _ptr(self.targets), 1, _ptr(self.g_image),
-                   _ptr(self.loss), s)
+        if self.background is None:
+            self._call("ngt_raymarch_fwd_l2", ctypes.byref(self.ray), _ptr(self.targets), 1, _ptr(self.g_image),
+                       _ptr(self.loss), s)
+        else:
+            self._call("ngt_raymarch_fwd_l2_background", ctypes.byref(self.ray), _ptr(self.background),
+                       _ptr(self.targets), 1, _ptr(self.g_image), _ptr(self.loss), s)
 
     def launch(self):
         """Enqueue forward + loss + backward on the current stream."""

@@ -38,13 +38,25 @@ def centered_velocity_adjoint(g_uc, shapes):
     return gx, gy, gz
 
 
-def _idx(shape, dt):
+def _idx(shape, dt, z0=0):
     d, h, w = shape
-    z, y, x = np.meshgrid(np.arange(d), np.arange(h), np.arange(w), indexing="ij")
+    z, y, x = np.meshgrid(np.arange(z0, z0 + d), np.arange(h), np.arange(w), indexing="ij")
     return np.stack([x, y, z], -1).astype(dt)
 
 
-def maccormack(data, lut, order=2, clamp="MC_SMOOTH", boundary="CLAMP", return_state=False):
+def _positions(lut, shape, dt, z0, sign):
+    """Sample positions ``sign * lut + index`` of a lattice whose first plane is
+    global plane ``z0``, returned relative to that plane: the global position
+    is formed first (the arithmetic of the whole-grid warp) and ``z0`` then
+    subtracted, which is exact, so a slab ``data[z0:z0+d]`` is sampled at the
+    same fractions as the whole grid."""
+    p = (lut if sign > 0 else -lut) + _idx(shape, dt, z0)
+    if z0:
+        p[..., 2] -= dt.type(z0)
+    return p
+
+
+def maccormack(data, lut, order=2, clamp="MC_SMOOTH", boundary="CLAMP", return_state=False, z0=0):
     """Warp ``data`` (D,H,W,C) by a relative lookup ``lut`` (D,H,W,3) on the same
     lattice (``VelocityGrid.warp`` data_structures.py:1690-1737 /
     ``_warp_vel_component`` :1081-1106).
@@ -53,15 +65,20 @@ def maccormack(data, lut, order=2, clamp="MC_SMOOTH", boundary="CLAMP", return_s
     order 2: ``back = S(fwd, idx-lut)``; ``corr = fwd + 0.5*(data-back)``; with
     MC_SMOOTH the voxels where ``corr`` leaves the [min, max] of the forward
     lookup's 8 corners revert to ``fwd``.  ``clamp='NEGATIVE'`` applies max(.,0).
+
+    ``z0``: ``data`` and ``lut`` are planes z0.. of a larger grid (a slab cut with
+    a halo by a caller that splits the warp over processes); positions are then
+    formed with global indices as in the whole-grid warp.  The slab's own edge
+    planes see the boundary rule, so only planes a trace cannot carry past the
+    slab edge match the whole-grid result.
     """
     dt = data.dtype
-    idx = _idx(data.shape[:3], dt)
-    p1 = lut + idx
+    p1 = _positions(lut, data.shape[:3], dt, z0, 1)
     fwd = core.read_linear(data, p1, boundary)
     st = {"p1": p1, "fwd": fwd}
     out = fwd
     if order == 2:
-        p2 = (-lut) + idx
+        p2 = _positions(lut, data.shape[:3], dt, z0, -1)
         back = core.read_linear(fwd, p2, boundary)
         corr = fwd + dt.type(0.5) * (data - back)
         st.update(p2=p2, back=back, corr=corr)
@@ -95,15 +112,16 @@ def _scatter(grid_like, p, g, boundary, mode):
     return gx
 
 
-def maccormack_grad(data, lut, grad_out, order=2, clamp="MC_SMOOTH", boundary="CLAMP", grad_mode="exact"):
+def maccormack_grad(data, lut, grad_out, order=2, clamp="MC_SMOOTH", boundary="CLAMP", grad_mode="exact", z0=0):
     """Backward of :func:`maccormack`.  Returns (d_data, d_lut).
 
     ``exact``: adjoint of the composition (the MC_SMOOTH mask is piecewise constant,
     MIN/MAX lookups carry no gradient, as ``tf.less/tf.greater`` give none).
     ``reference``: the same TF composition but each LUT-resample adjoint is the
-    reference's count-normalised scatter (``ops_loader.py:41-58``)."""
+    reference's count-normalised scatter (``ops_loader.py:41-58``).
+    ``z0``: slab origin as in :func:`maccormack`."""
     dt = data.dtype
-    out, st = maccormack(data, lut, order, clamp, boundary, return_state=True)
+    out, st = maccormack(data, lut, order, clamp, boundary, return_state=True, z0=z0)
     g = np.asarray(grad_out, dt)
     if clamp == "NEGATIVE":
         g = np.where(st["pre_neg"] >= 0, g, 0)

@@ -352,21 +352,24 @@ def lod_transform(input_shape, matrix_mv, matrix_p, frustum_params, output_shape
 
 # ------------------------------------------------------------------------ raymarch
 
-def ray_setup(cam, in_xyz, out_dims_zyx, boundary):
+def ray_setup(cam, in_xyz, out_dims_zyx, boundary, rows=None):
     """Per-pixel ray start, step and step count (``getRaymarchStep``,
     raymarch_grid.cu.cc:109-200), in float64.  Returns start (H,W,3), step (H,W,3),
-    steps (H,W) int, hit (H,W) bool and the far end used by the reference backward."""
+    steps (H,W) int, hit (H,W) bool and the far end used by the reference backward.
+    ``rows = (y0, y1)`` restricts the rays to image rows y0..y1-1 of the full
+    H x W image (the arrays then have y1 - y0 rows)."""
     D, H, W = out_dims_zyx
     dims = np.array([W, H, D], dtype=np.float64)
     zmax = float(max(D - 1, 1))
-    y, x = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    y0, y1 = (0, H) if rows is None else (int(rows[0]), int(rows[1]))
+    y, x = np.meshgrid(np.arange(y0, y1), np.arange(W), indexing="ij")
     i0 = np.stack([x + 0.5, y + 0.5, np.full(x.shape, 0.5)], -1)
     i1 = np.stack([x + 0.5, y + 0.5, np.full(x.shape, zmax + 0.5)], -1)
     start = core.idx_to_os(i0, dims, cam)
     end = core.idx_to_os(i1, dims, cam)
     step = (end - start) / zmax
-    steps = np.full((H, W), D, dtype=np.int64)
-    hit = np.ones((H, W), bool)
+    steps = np.full(x.shape, D, dtype=np.int64)
+    hit = np.ones(x.shape, bool)
     if boundary == BORDER:
         d = end - start
         rd = d / np.linalg.norm(d, axis=-1, keepdims=True)
@@ -413,9 +416,10 @@ def _v2_sample(grid, pos, interpolation, boundary):
 
 def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape,
                             interpolation=LINEAR, boundary=BORDER, blending_mode="BEER_LAMBERT",
-                            keep_dims=False, separate_camera_batch=True):
+                            keep_dims=False, separate_camera_batch=True, rows=None):
     """Forward of ``RaymarchGridTransform`` (raymarch_grid.cc:29-63, 208-313;
-    raymarch_grid.cu.cc:202-252, 359-433).  input NDHWC -> NVHWC (NV1HWC with keep_dims)."""
+    raymarch_grid.cu.cc:202-252, 359-433).  input NDHWC -> NVHWC (NV1HWC with keep_dims).
+    ``rows = (y0, y1)``: only image rows y0..y1-1 (output height y1 - y0)."""
     x = np.asarray(input)
     dt = x.dtype
     M, Vm, P, F = _mats(matrix_m), _mats(matrix_v), _mats(matrix_p), _frusta(frustum_params)
@@ -423,12 +427,13 @@ def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params,
     D, H, W = (int(s) for s in output_shape)
     C = x.shape[-1]
     in_xyz = core.dims_xyz(x[0])
-    out = np.zeros((N, V if separate_camera_batch else 1, H, W, C), dt)
+    Hr = H if rows is None else int(rows[1]) - int(rows[0])
+    out = np.zeros((N, V if separate_camera_batch else 1, Hr, W, C), dt)
     for b, c, slot in _camera_loop(N, V, separate_camera_batch):
         cam = core.CameraMatrices(M[b], Vm[c], P[c], F[c])
-        start, step, steps, hit, _ = ray_setup(cam, in_xyz, (D, H, W), boundary)
+        start, step, steps, hit, _ = ray_setup(cam, in_xyz, (D, H, W), boundary, rows)
         pos = _ray_positions(start, step, steps, dt)
-        acc = np.zeros((H, W, C), dt)
+        acc = np.zeros((Hr, W, C), dt)
         for i in range(pos.shape[0]):
             active = (i < steps) & hit
             s = _v2_sample(x[b], pos[i], interpolation, boundary)
@@ -443,14 +448,17 @@ def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params,
 def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v, matrix_p,
                                  frustum_params, output_shape, interpolation=LINEAR, boundary=BORDER,
                                  blending_mode="BEER_LAMBERT", keep_dims=False,
-                                 separate_camera_batch=True, grad_mode="exact"):
+                                 separate_camera_batch=True, grad_mode="exact", rows=None):
     """Gradient of ``RaymarchGridTransform`` (raymarch_grid.cc:67-92, 363-497;
     raymarch_grid.cu.cc:458-724).
 
     ``reference``: back-to-front from the far end with ``pos -= step`` (for BORDER a
     different lattice than the forward's), accumulator rebuilt by subtraction,
     scatter weighted and divided per voxel by the summed weights, per camera.
-    ``exact``: the adjoint of the forward at the forward's own sample positions."""
+    ``exact``: the adjoint of the forward at the forward's own sample positions.
+    ``rows = (y0, y1)``: the rays of image rows y0..y1-1 only (``output`` and
+    ``output_grad`` hold those rows); the exact gradients of row bands add up to
+    the full image's."""
     if interpolation != LINEAR:
         raise NotImplementedError("raymarch gradients support LINEAR interpolation only")
     x = np.asarray(input)
@@ -467,7 +475,7 @@ def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v,
     gx = np.zeros_like(x)
     for b, c, slot in _camera_loop(N, V, separate_camera_batch):
         cam = core.CameraMatrices(M[b], Vm[c], P[c], F[c])
-        start, step, steps, hit, end = ray_setup(cam, in_xyz, (D, H, W), boundary)
+        start, step, steps, hit, end = ray_setup(cam, in_xyz, (D, H, W), boundary, rows)
         g = gy[b, slot]
         if grad_mode == "exact":
             pos = _ray_positions(start, step, steps, dt)
@@ -577,3 +585,27 @@ def reduce_grid_blend_grad(output_grad, output, input, blending_mode="BEER_LAMBE
         d, grads, prev = core.blend_gradients_reference(grads, x[:, i], prev, blending_mode)
         gx[:, i] = d
     return gx
+
+
+# ---------------------------------------------------------- background composite
+
+def background_composite(image, background):
+    """Background composite of ``Renderer.render_density`` (renderer.py:779-781,
+    804-806): ``t = exp(-image[..., -1:])``, the alpha channel cut, and
+    ``image[..., :-1] + background * t``; ``background`` broadcasts to the
+    per-camera image (V, H, W, C - 1) and is shared by the batch."""
+    x = np.asarray(image)
+    t = np.exp(-x[..., -1:])
+    return x[..., :-1] + np.asarray(background, x.dtype) * t
+
+
+def background_composite_grad(image, background, output_grad):
+    """Adjoint of :func:`background_composite`: (d image, d background), the latter
+    summed over the batch."""
+    x = np.asarray(image)
+    g = np.asarray(output_grad, x.dtype)
+    b = np.broadcast_to(np.asarray(background, x.dtype), x.shape[1:-1] + (x.shape[-1] - 1,))
+    t = np.exp(-x[..., -1:])
+    gi = np.concatenate([g, -t * (b * g).sum(-1, keepdims=True)], -1)
+    gb = (t * g).sum(0)
+    return gi, gb

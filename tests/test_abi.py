@@ -356,3 +356,32 @@ def test_misaligned_buffers_rejected(lib):
     assert lib.ngt_image_l2_loss(L.F32, 4, 2, 1, ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1001),
                                  ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000), None) == L.NGT_ERR_INVALID_ARGUMENT
     assert b"target" in lib.ngt_last_error_message()
+
+
+def test_background_validation(lib):
+    """The background composite and the fused loss with a background reject bad
+    sizes, channel counts and pointers before any device work."""
+    from ngt_gb300 import _lib as L
+    ok = ctypes.c_void_p(0x1000)
+    assert lib.ngt_background_composite(L.F32, 1, 16, 3, ok, ok, ok, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_background_composite(L.F32, 0, 16, 2, ok, ok, ok, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_background_composite(L.F32, 1, 16, 2, ok, None, ok, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_background_composite(L.BF16, 1, 16, 2, ok, ok, ok, None) == L.NGT_ERR_UNSUPPORTED
+    assert lib.ngt_background_composite_bwd(L.F32, 1, 16, 2, ok, ok, ok, None, None, None) == \
+        L.NGT_ERR_INVALID_ARGUMENT
+    r = L.RaymarchArgs()
+    r.dtype = L.F32
+    r.input_shape = L.I64x5(1, 4, 4, 4, 1)
+    r.output_dhw = L.I64x3(4, 4, 4)
+    for f in ("input", "output", "matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(r, f, ok)
+    r.num_cameras = 1
+    r.interpolation, r.boundary, r.blending_mode, r.separate_camera_batch = 1, 0, 0, 1
+    r.emission_channels = 2
+    fn = lib.ngt_raymarch_fwd_l2_background
+    assert fn(ctypes.byref(r), None, ok, 1, ok, ok, None) == L.NGT_ERR_INVALID_ARGUMENT  # no background
+    assert fn(ctypes.byref(r), ok, ok, 2, ok, ok, None) == L.NGT_ERR_INVALID_ARGUMENT  # loss on the depth channel
+    r.blending_mode = 4
+    assert fn(ctypes.byref(r), ok, ok, 1, ok, ok, None) == L.NGT_ERR_UNSUPPORTED  # not Beer-Lambert
+    r.blending_mode, r.emission_channels = 0, 0
+    assert fn(ctypes.byref(r), ok, ok, 1, ok, ok, None) == L.NGT_ERR_INVALID_ARGUMENT  # one blend channel

@@ -1,6 +1,6 @@
 """Host-side pieces of bench.py that need no GPU: the clock-sample parsing, the
-peak lookup, the reference arm's sample plan, and the reference arm's JSON line
-(with a stand-in for the timed CPU step)."""
+peak lookup, and the reference arm's JSON line (with a stand-in for the timed
+CPU step)."""
 import io
 import json
 import os
@@ -48,35 +48,52 @@ def test_measured_peak_fallback(tmp_path, monkeypatch):
     assert bench.measured_peak_hbm() == (6798.9, "measured")
 
 
-def test_reference_sample_plan():
-    assert bench.reference_sample_plan(5) == (48, 4)
-    assert bench.reference_sample_plan(405) == (32, 2)
+class _FakePool:
+    def close(self):
+        pass
+
+    def join(self):
+        pass
 
 
 def test_reference_arm_line(monkeypatch):
-    """The reference arm's line carries the contract's keys, and stops timing at
-    its budget (here: after the first timed step)."""
+    """The reference arm's line carries the contract's keys, times full steps
+    (``cpu_step``) after the warm-up ones, and stops timing at its budget (here:
+    after the first timed step)."""
     import argparse
     calls = []
 
-    def fake(procs, adv_n=64, rows=8, pool=None):
-        calls.append((adv_n, rows))
-        return 20.0, {"advect_sample": "a", "render_sample": "r"}
+    def fake(pool, nproc, w, targets):
+        calls.append((nproc, w, targets))
+        return 20.0
 
-    monkeypatch.setattr(bench, "cpu_step_time", fake)
+    monkeypatch.setattr(bench, "reference_setup", lambda: (_FakePool(), 3, "w", "t"))
+    monkeypatch.setattr(bench, "cpu_step", fake)
     monkeypatch.setattr(bench, "REFERENCE_BUDGET_S", -1.0)
-    monkeypatch.setattr(os, "cpu_count", lambda: 1)
     buf = io.StringIO()
     with redirect_stdout(buf):
         bench.reference_arm(argparse.Namespace(impl="reference", gpus=1, steps=400, warmup=2), 1, 0)
     line = json.loads(buf.getvalue().strip().splitlines()[-1])
-    assert len(calls) == 3 and calls[0] == (32, 2)
+    assert len(calls) == 3 and calls[0] == (3, "w", "t")
     assert line["impl"] == "reference" and line["steps"] == 400 and line["steps_timed"] == 1
     assert abs(line["value"] - 0.05) < 1e-12 and line["unit"] == "steps/s" and line["higher_is_better"]
-    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 1
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 3
+    assert "full step" in line["cpu_baseline"]["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
-    assert line["cpu_baseline"]["host"]["logical_cpus"] == 1
+    assert line["timed_s"] == 20.0
+
+
+def test_cpu_step_runs_the_oracle_step(monkeypatch):
+    """cpu_step times one call of the oracle's full step on the given pool."""
+    from oracle import parallel
+    seen = []
+    monkeypatch.setattr(parallel, "render_advect_step", lambda *a, **k: seen.append(a[:2]))
+
+    class W:
+        rho = ux = uy = uz = M = V = P = F = image_dhw = depth_step = None
+    t = bench.cpu_step("pool", 7, W(), None)
+    assert seen == [("pool", 7)] and t >= 0.0
 
 
 def test_host_cpu_description(tmp_path):

@@ -1,0 +1,204 @@
+"""Parity with the oracle at the benchmark configurations' own sizes.
+
+The CUDA operators against the NumPy oracle (restating the reference kernels'
+semantics; raymarch_grid.cu.cc:202-252, 482-521, resample_grid.cu.cc:255-267,
+604-623, reduce_blend.cu.cc:34-80, data_structures.py:1690-1737) on the seeded
+synthetic inputs of each configuration, in full:
+
+1. plain forward ops at 64^3: transform resample into the 64 x 128 x 128 frustum
+   grid, its depth blend to the 128 x 128 image, the fused raymarch of the same
+   camera, the semi-Lagrangian warp and its LUT resample;
+2. the differentiated step at 128^3 with all 5 views of 256 x 256 x 128;
+3. the checkpointed chain on the full 96 x 176 x 96 plume grid, 12 frames with
+   checkpoints every 5 (two segment boundaries inside the chain);
+4. the 32 uneven scenes of seed 4 through the batched step.
+
+Bars: LUT resample and advection forward bit for bit; transform resample,
+depth blend, raymarch images and losses 1e-5 and every gradient 1e-4 relative
+L2 (the stated forward / gradient tolerances).  The oracle runs split over the
+host's processes (``oracle.parallel``).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import advect as oadvect
+from oracle import ops as oops
+from oracle import parallel
+
+pytestmark = pytest.mark.gpu
+
+FWD_TOL = 1e-5
+GRAD_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def pool():
+    p, n = parallel.make_pool()
+    yield p, n
+    p.close()
+    p.join()
+
+
+def dev():
+    return torch.device("cuda", 0)
+
+
+def T(a, dtype=torch.float32):
+    return torch.as_tensor(np.ascontiguousarray(a), device=dev()).to(dtype)
+
+
+def rel(a, b):
+    a = a.detach().double().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a, np.float64)
+    b = b.detach().double().cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b, np.float64)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+# ------------------------------------------------------------------ config 1
+def test_config1_plain_forward_ops():
+    """64^3 blobs, one camera (fov 40, 1.3 x diagonal) into 64 x 128 x 128, the
+    renderer's [light*step, step] grid: resample, depth blend, fused raymarch;
+    one semi-Lagrangian step (dt 1, CLAMP) and its LUT resample."""
+    from ngt_gb300 import advect, ops, workloads
+    w = workloads.config1_small()
+    s = np.float32(w.depth_step)
+    x = (w.rho * np.asarray([s, s], np.float32))[None]  # (1, 64, 64, 64, 2)
+    xs = oops.sample_grid_transform(x, w.M, w.V, w.P, w.F, w.image_dhw)
+    xg = ops.sample_grid_transform(T(x), w.M, w.V, w.P, w.F, w.image_dhw)
+    assert xg.shape == (1, 1) + tuple(w.image_dhw) + (2,)
+    assert rel(xg, xs) < FWD_TOL
+    blend = oops.reduce_grid_blend(xs[0])
+    assert rel(ops.reduce_grid_blend(xg[0]), blend) < FWD_TOL
+    img = oops.raymarch_grid_transform(x, w.M, w.V, w.P, w.F, w.image_dhw)
+    assert rel(ops.raymarch_grid_transform(T(x), w.M, w.V, w.P, w.F, w.image_dhw), img) < FWD_TOL
+    img1 = oops.raymarch_grid_transform(w.rho[None], w.M, w.V, w.P, w.F, w.image_dhw)
+    got1 = ops.raymarch_grid_transform(T(w.rho[None]), w.M, w.V, w.P, w.F, w.image_dhw, emission_scale=(s, s))
+    assert rel(got1, img1 * np.asarray([s, s], np.float32)) < FWD_TOL
+    # semi-Lagrangian warp (order 1) and the LUT resample it is made of: bit for bit
+    sl = oadvect.density_maccormack(w.rho, w.ux, w.uy, w.uz, order=1, clamp="NONE")
+    got = advect.warp(T(w.rho), T(w.ux), T(w.uy), T(w.uz), dt=1.0, order=1, clamp="NONE", boundary="CLAMP")
+    assert np.array_equal(got.cpu().numpy(), sl)
+    lut = oadvect.centered_velocity(w.ux, w.uy, w.uz) * np.float32(-1.0)
+    lut4 = np.concatenate([lut, np.zeros(lut.shape[:3] + (1,), np.float32)], -1)[None]
+    want = oops.sample_grid_lut(w.rho[None], lut4, boundary=oops.CLAMP)
+    got = ops.sample_grid_lut(T(w.rho[None]), T(lut4), boundary="CLAMP")
+    assert np.array_equal(got.cpu().numpy(), want)
+    assert np.array_equal(want[0, 0], sl)
+
+
+def test_config1_gradients():
+    """The registered (exact) gradients of the same ops at the same size."""
+    from ngt_gb300 import ops, workloads
+    w = workloads.config1_small()
+    s = np.float32(w.depth_step)
+    x = (w.rho * np.asarray([s, s], np.float32))[None]
+    rng = np.random.default_rng(21)
+    gs = rng.standard_normal((1, 1) + tuple(w.image_dhw) + (2,)).astype(np.float32)
+    want = oops.sample_grid_transform_grad(x, gs, w.M, w.V, w.P, w.F)
+    got = ops.sample_grid_transform_grad(T(x), T(gs), w.M, w.V, w.P, w.F)
+    assert rel(got, want) < GRAD_TOL
+    img = oops.raymarch_grid_transform(x, w.M, w.V, w.P, w.F, w.image_dhw)
+    gi = rng.standard_normal(img.shape).astype(np.float32)
+    want = oops.raymarch_grid_transform_grad(x, img, gi, w.M, w.V, w.P, w.F, w.image_dhw)
+    got = ops.raymarch_grid_transform_grad(T(x), T(img), T(gi), w.M, w.V, w.P, w.F, w.image_dhw)
+    assert rel(got, want) < GRAD_TOL
+    g = rng.standard_normal(w.rho.shape).astype(np.float32)
+    want = oadvect.density_maccormack_grad(w.rho, w.ux, w.uy, w.uz, g, order=1, clamp="NONE")
+    from ngt_gb300 import advect
+    ts = [T(a).requires_grad_() for a in (w.rho, w.ux, w.uy, w.uz)]
+    out = advect.warp(*ts, dt=1.0, order=1, clamp="NONE", boundary="CLAMP")
+    out.backward(T(g))
+    for t, b in zip(ts, want):
+        assert rel(t.grad, b) < GRAD_TOL
+
+
+# ------------------------------------------------------------------ config 2
+def test_config2_full_step(pool):
+    """128^3, MacCormack (MC_SMOOTH), 5 views of 256 x 256 x 128, image L2,
+    backward to the density and the three face grids: the fused step against
+    the oracle's composition on the same inputs and targets."""
+    from ngt_gb300 import workloads
+    from ngt_gb300.step import RenderAdvectStep
+    p, n = pool
+    w = workloads.config2()
+    tgt, _, _ = parallel.render_l2(p, n, w.rho_target, w.depth_step, w.M, w.V, w.P, w.F, w.image_dhw)
+    tgt = np.ascontiguousarray(tgt[..., :1])
+    step = RenderAdvectStep(T(w.rho), T(w.ux), T(w.uy), T(w.uz), w.M, w.V, w.P, w.F, T(tgt), w.image_dhw)
+    loss = float(step.step().item())
+    image, ref_loss, ref = parallel.render_advect_step(p, n, w.rho, w.ux, w.uy, w.uz, w.M, w.V, w.P, w.F, tgt,
+                                                       w.image_dhw, w.depth_step)
+    assert rel(step.image, image) < FWD_TOL
+    assert abs(loss - ref_loss) <= FWD_TOL * abs(ref_loss)
+    for a, b in zip(step.gradients(), ref):
+        assert rel(a, b) < GRAD_TOL
+
+
+# ------------------------------------------------------------------ config 3
+def test_config3_full_grid_chain(pool):
+    """The plume chain on its full 96 x 176 x 96 grid with its 192 x 192 x 96
+    camera, 12 frames, checkpoints every 5: loss and the gradients to the
+    initial density and the velocity against the oracle run frame by frame."""
+    from ngt_gb300 import workloads
+    from ngt_gb300.chain import AdvectRenderChain, chain_targets
+    p, n = pool
+    w = workloads.plume_chain(frames=12)
+    u = [T(w.ux), T(w.uy), T(w.uz)]
+    tg = chain_targets(T(w.rho0_target), *u, T(w.source), w.M, w.V, w.P, w.F, w.image_dhw, w.frames)
+    ch = AdvectRenderChain(T(w.rho0), *u, T(w.source), w.M, w.V, w.P, w.F, tg, w.image_dhw, w.frames,
+                           checkpoint_every=5)
+    loss = float(ch.run().item())
+    targets = tg.cpu().numpy()
+    rhos = [w.rho0]
+    ref_loss = 0.0
+    g_render = []
+    for t in range(w.frames):
+        rhos.append(parallel.density_fwd(p, n, rhos[-1], w.ux, w.uy, w.uz) + w.source)
+        _, l, g = parallel.render_l2(p, n, rhos[-1], w.depth_step, w.M, w.V, w.P, w.F, w.image_dhw,
+                                     targets[t][None])
+        ref_loss += l
+        g_render.append(g)
+    g = np.zeros_like(w.rho0)
+    gu = [np.zeros_like(a) for a in (w.ux, w.uy, w.uz)]
+    for t in range(w.frames - 1, -1, -1):
+        g = g + g_render[t]
+        g, *gv = parallel.density_bwd(p, n, rhos[t], w.ux, w.uy, w.uz, g)
+        for a, b in zip(gu, gv):
+            a += b
+    assert abs(loss - ref_loss) <= FWD_TOL * abs(ref_loss)
+    for a, b in zip(ch.gradients(), [g] + gu):
+        assert rel(a, b) < GRAD_TOL
+
+
+# ------------------------------------------------------------------ config 4
+def test_config4_seed4_batch(pool):
+    """The 32 scenes of seed 4 (axes 48-160, 1-8 cameras, images 64-256, depth
+    32-128): semi-Lagrangian warp, render, image L2 and backward per scene,
+    through the batched step, against the oracle scene by scene."""
+    from ngt_gb300 import ops, workloads
+    from ngt_gb300.batch import BatchedScenes, Scene
+    p, n = pool
+    ws = workloads.config4()
+    sc, tgts = [], []
+    for w in ws:
+        with torch.no_grad():
+            tgt = ops.raymarch_grid_transform(T(w.rho_target)[None], w.M, w.V, w.P, w.F, w.image_dhw,
+                                              emission_scale=(w.depth_step, w.depth_step))[..., :1]
+        tgts.append(tgt.cpu().numpy())
+        sc.append(Scene(T(w.rho), T(w.ux), T(w.uy), T(w.uz), w.M, w.V, w.P, w.F, w.image_dhw, tgt))
+    b = BatchedScenes(sc)
+    b.launch()
+    torch.cuda.synchronize()
+    images = b.images.cpu().numpy()
+    loss = float(b.loss.item())
+    ref_loss, off = 0.0, 0
+    for k, w in enumerate(ws):
+        rho2 = parallel.density_fwd(p, n, w.rho, w.ux, w.uy, w.uz, order=1, clamp="NONE")
+        img, l, g_rho2 = parallel.render_l2(p, n, rho2, w.depth_step, w.M, w.V, w.P, w.F, w.image_dhw, tgts[k])
+        ref_loss += l
+        npx = img.shape[1] * img.shape[2] * img.shape[3]
+        assert rel(images[off:off + npx], img.reshape(-1, 2)) < FWD_TOL, k
+        off += npx
+        ref = parallel.density_bwd(p, n, w.rho, w.ux, w.uy, w.uz, g_rho2, order=1, clamp="NONE")
+        for a, r in zip(b.gradients(k), ref):
+            assert rel(a, r) < GRAD_TOL, k
+    assert abs(loss - ref_loss) <= FWD_TOL * abs(ref_loss)

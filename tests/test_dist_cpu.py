@@ -62,7 +62,15 @@ def _reference_rank(rank, world, port, out):
 
     import bench
     called = []
-    bench.cpu_step_time = lambda *a, **k: called.append(1) or (1.0, {"advect_sample": "s", "render_sample": "s"})
+    class _Pool:
+        def close(self):
+            pass
+
+        def join(self):
+            pass
+
+    bench.reference_setup = lambda: (_Pool(), 1, None, None)
+    bench.cpu_step = lambda *a, **k: called.append(1) or 1.0
     args = argparse.Namespace(impl="reference", gpus=world, steps=1, warmup=0)
     w, r, _ = bench.dist_init(args)
     buf = io.StringIO()
