@@ -314,6 +314,7 @@ def gpu_arm(args, world, rank, local):
         kernel = kernel_stats(step, torch, dev, w, st, max(10, args.steps // 2), flush)
 
     e2e = e2e_measure(torch, dev, w, st, tgt, args, flush)
+    e2e_ops = e2e_measure(torch, dev, w, st, tgt, args, flush, fused=False)
     e2e_step = e2e_step_measure(torch, step, w, st, args, flush) if not args.no_graph else None
     samples = 2 * 2 * 128 ** 3 + 2 * 5 * 256 * 256 * 128
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
@@ -343,6 +344,7 @@ def gpu_arm(args, world, rank, local):
     if clk:
         line["clocks"] = clk
     line["e2e"] = e2e
+    line["e2e_ops"] = e2e_ops
     if e2e_step:
         line["e2e_step"] = e2e_step
     if rank == 0 and world == 1 and args.cpu_baseline == "on":
@@ -401,19 +403,26 @@ def kernel_stats(step, torch, dev, w, st, iters, flush):
     return name, tot[name] / iters, nbytes[name]
 
 
-def e2e_measure(torch, dev, w, st, tgt, args, flush):
+def e2e_measure(torch, dev, w, st, tgt, args, flush, fused=True):
     """Same step through the public autograd API, with the density and velocity
-    copied from pinned host memory every step and the loss read back."""
+    copied from pinned host memory every step and the loss read back.  fused:
+    the one differentiable call ``step.render_advect_loss``; else the three
+    operators ``advect.warp`` -> ``ops.raymarch_grid_transform`` ->
+    ``ops.image_l2_loss`` with autograd between them."""
     from ngt_gb300 import advect, ops
+    from ngt_gb300.step import render_advect_loss
     host = [torch.as_tensor(a).to(st).pin_memory() for a in (w.rho, w.ux, w.uy, w.uz)]
     h2d = sum(t.numel() * t.element_size() for t in host)
     scale = (w.depth_step, w.depth_step)
 
     def one():
         ts = [t.to(dev, non_blocking=True).requires_grad_() for t in host]
-        r2 = advect.warp(ts[0], ts[1], ts[2], ts[3], dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP")
-        img = ops.raymarch_grid_transform(r2[None], w.M, w.V, w.P, w.F, w.image_dhw, emission_scale=scale)
-        loss = ops.image_l2_loss(img, tgt)
+        if fused:
+            loss = render_advect_loss(ts[0], ts[1], ts[2], ts[3], w.M, w.V, w.P, w.F, tgt, w.image_dhw)
+        else:
+            r2 = advect.warp(ts[0], ts[1], ts[2], ts[3], dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP")
+            img = ops.raymarch_grid_transform(r2[None], w.M, w.V, w.P, w.F, w.image_dhw, emission_scale=scale)
+            loss = ops.image_l2_loss(img, tgt)
         loss.backward()
         return float(loss.item())
 
@@ -428,9 +437,9 @@ def e2e_measure(torch, dev, w, st, tgt, args, flush):
         t0 = time.perf_counter()
         one()
         tot += time.perf_counter() - t0
-    return {"value": n / tot, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4,
-            "path": "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + ops.image_l2_loss, "
-                    "loss.backward()"}
+    path = ("ngt_gb300.step.render_advect_loss (one autograd node), loss.backward()" if fused else
+            "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + ops.image_l2_loss, loss.backward()")
+    return {"value": n / tot, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4, "path": path}
 
 
 def e2e_step_measure(torch, step, w, st, args, flush):

@@ -144,8 +144,16 @@ typedef struct {
   const void* output_grad;
   void* input_grad;
   int32_t grad_mode;
-  void* workspace;            /* per-voxel sample counts (reference mode) */
+  void* workspace;            /* per-voxel sample counts (reference mode) / cameras and
+                                 gather buckets (deterministic) */
   size_t workspace_bytes;
+  /* Exact LINEAR mode: nonzero computes the input gradient in gather form
+   * (bit-reproducible): the frustum samples are bucketed by the cell of their
+   * lower corner (counting sort) and every voxel sums the samples of its 8
+   * neighbouring buckets in sample order, in place of the reference's float
+   * atomics (resample_grid.cu.cc:1160-1190).  Fewer than 2^31 samples per
+   * batch entry. */
+  int32_t deterministic;
 } ngt_sample_transform_grad_args;
 
 int ngt_sample_transform_fwd(const ngt_sample_transform_args* args, void* stream);
@@ -217,6 +225,13 @@ typedef struct {
    * instead of building their own.  Null: built per call.  The batch entry
    * points build their own and reject it. */
   const void* quad;
+  /* Optional: every ray's start, step and sample count, prepared by
+   * ngt_raymarch_rays for these matrices, frustum, image and grid sizes and
+   * boundary (static cameras across calls).  Those are set up in double
+   * precision and rounded once, so the march starts from the float nearest the
+   * exact start; null: set up per ray in float arithmetic.  Used by the forward
+   * and the exact backward. */
+  const void* rays;
 } ngt_raymarch_args;
 
 typedef struct {
@@ -236,6 +251,17 @@ typedef struct {
    * writing it (a gradient summed over several renders of one grid, e.g. the
    * frames of a chain).  The reference's ops write their outputs. */
   int32_t accumulate;
+  /* Exact mode: nonzero makes the input gradient bit-reproducible.  The
+   * reference's scatter (raymarch_grid.cu.cc:482-521) adds float atomics in
+   * an order that varies from run to run; here every sample's contribution is
+   * rounded to a 64-bit fixed-point integer whose scale a first pass over the
+   * rays chooses (the largest contribution times the ray-sample count stays
+   * below 2^62, so no sum overflows and each contribution is resolved to
+   * 2^-36 of the largest at 2^26 samples), the integers are summed with
+   * integer atomics (associative: the same sums in every run) and converted
+   * once.  Direct gathers, two extra passes over the rays; the workspace holds
+   * one 64-bit integer per input cell and channel. */
+  int32_t deterministic;
 } ngt_raymarch_grad_args;
 
 size_t ngt_raymarch_fwd_workspace_bytes(const ngt_raymarch_args* args);
@@ -255,6 +281,13 @@ int ngt_raymarch_fwd(const ngt_raymarch_args* args, void* stream);
  * ngt_raymarch_quad fails with NGT_ERR_UNSUPPORTED.  No counterpart in the
  * reference, whose kernels gather the eight corners per sample
  * (sampling_v2.hpp:37-124). */
+/* The ray table of args (32 bytes per (batch, camera) slot and pixel, 16-byte
+ * aligned): the ray set-up of getRaymarchStep / RayGridIntersectionDistances
+ * (raymarch_grid.cu.cc:109-200) in double precision, rounded to the float start
+ * and step the march accumulates.  No counterpart in the reference, which sets
+ * up every ray in float arithmetic in each kernel. */
+size_t ngt_raymarch_rays_bytes(const ngt_raymarch_args* args);
+int ngt_raymarch_rays(const ngt_raymarch_args* args, void* rays, void* stream);
 size_t ngt_raymarch_quad_bytes(const ngt_raymarch_args* args);
 int ngt_raymarch_quad(const ngt_raymarch_args* args, void* quad, void* stream);
 int ngt_raymarch_bwd(const ngt_raymarch_grad_args* args, void* stream);

@@ -48,7 +48,7 @@ class SampleTransformArgs(ctypes.Structure):
 
 class SampleTransformGradArgs(ctypes.Structure):
     _fields_ = [("fwd", SampleTransformArgs), ("output_grad", c_vp), ("input_grad", c_vp), ("grad_mode", c_i32),
-                ("workspace", c_vp), ("workspace_bytes", c_sz)]
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("deterministic", c_i32)]
 
 
 class LodArgs(ctypes.Structure):
@@ -63,12 +63,13 @@ class RaymarchArgs(ctypes.Structure):
                 ("num_cameras", c_i32), ("output", c_vp), ("interpolation", c_i32), ("boundary", c_i32),
                 ("blending_mode", c_i32), ("keep_dims", c_i32), ("separate_camera_batch", c_i32),
                 ("emission_channels", c_i32), ("emission_scale", c_f32 * 4), ("workspace", c_vp),
-                ("workspace_bytes", c_sz), ("cameras", c_vp), ("quad", c_vp)]
+                ("workspace_bytes", c_sz), ("cameras", c_vp), ("quad", c_vp), ("rays", c_vp)]
 
 
 class RaymarchGradArgs(ctypes.Structure):
     _fields_ = [("fwd", RaymarchArgs), ("output", c_vp), ("output_grad", c_vp), ("input_grad", c_vp),
-                ("grad_mode", c_i32), ("workspace", c_vp), ("workspace_bytes", c_sz), ("accumulate", c_i32)]
+                ("grad_mode", c_i32), ("workspace", c_vp), ("workspace_bytes", c_sz), ("accumulate", c_i32),
+                ("deterministic", c_i32)]
 
 
 class ReduceBlendArgs(ctypes.Structure):
@@ -123,6 +124,8 @@ SIGNATURES = {
     "ngt_raymarch_fwd_workspace_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
     "ngt_raymarch_cameras_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
     "ngt_raymarch_cameras": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp], c_i32),
+    "ngt_raymarch_rays_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
+    "ngt_raymarch_rays": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp], c_i32),
     "ngt_raymarch_quad_bytes": ([ctypes.POINTER(RaymarchArgs)], c_sz),
     "ngt_raymarch_quad": ([ctypes.POINTER(RaymarchArgs), c_vp, c_vp], c_i32),
     "ngt_raymarch_fwd_l2": ([ctypes.POINTER(RaymarchArgs), c_vp, c_i32, c_vp, c_vp, c_vp], c_i32),

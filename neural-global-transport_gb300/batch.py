@@ -115,6 +115,11 @@ class BatchedScenes:
                                     device=dev))
             self._call("ngt_raymarch_cameras", ctypes.byref(r), _ptr(cams), self._stream())
             r.cameras = _ptr(cams)
+            # the scene's rays, set up once in double precision
+            rays = keep(torch.empty(int(self.lib.ngt_raymarch_rays_bytes(ctypes.byref(r))), dtype=torch.uint8,
+                                    device=dev))
+            self._call("ngt_raymarch_rays", ctypes.byref(r), _ptr(rays), self._stream())
+            r.rays = _ptr(rays)
             rg = self.ray_g[k]
             rg.fwd = r
             rg.output, rg.output_grad, rg.input_grad = _ptr(img), _ptr(gimg), _ptr(g_rho_adv)

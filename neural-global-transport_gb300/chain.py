@@ -141,12 +141,17 @@ class AdvectRenderChain:
         self.cameras = torch.empty(int(self.lib.ngt_raymarch_cameras_bytes(ctypes.byref(self.ray[0]))),
                                    dtype=torch.uint8, device=dev)
         self._call("ngt_raymarch_cameras", ctypes.byref(self.ray[0]), _ptr(self.cameras), self._stream())
+        # the rays of the fixed camera, set up once in double precision
+        self.rays = torch.empty(int(self.lib.ngt_raymarch_rays_bytes(ctypes.byref(self.ray[0]))), dtype=torch.uint8,
+                                device=dev)
+        self._call("ngt_raymarch_rays", ctypes.byref(self.ray[0]), _ptr(self.rays), self._stream())
         # render backward of segment slot j, its density gradient added to g_rho[k]
         self.ray_g = {}
         bws = 0
         for r in self.ray:
             r.workspace, r.workspace_bytes = _ptr(self.ray_fws), fws
             r.cameras = _ptr(self.cameras)
+            r.rays = _ptr(self.rays)
         for j, r in enumerate(self.ray):
             for k in range(2):
                 g = L.RaymarchGradArgs()

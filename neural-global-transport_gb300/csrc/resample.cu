@@ -348,6 +348,44 @@ __global__ void __launch_bounds__(kBlock) k_xf_bwd(XfParams<T> p, int reference)
   }
 }
 
+// Every slot's camera transform, one warp per slot, for the deterministic
+// adjoint's sample source.
+template <class T>
+__global__ void k_xf_cams(XfParams<T> p, Cam* __restrict__ cams) {
+  __shared__ Cam cam;
+  __shared__ CamScratch sh;
+  int b, c;
+  xf_slot(p, int(blockIdx.x), b, c);
+  build_cam_warp(p.M + 16 * b, p.V + 16 * c, p.P + 16 * c, p.F + 6 * c, cam, sh);
+  __syncwarp();
+  const float* src = reinterpret_cast<const float*>(&cam);
+  float* dst = reinterpret_cast<float*>(cams + blockIdx.x);
+  for (int i = threadIdx.x; i < int(sizeof(Cam) / sizeof(float)); i += 32) dst[i] = src[i];
+}
+
+// Samples of batch b for the deterministic input gradient: every (camera, output
+// voxel) of a slot that reads batch b, at the position k_xf_bwd scatters from.
+template <int C, class T>
+struct XfSource {
+  XfParams<T> p;
+  const Cam* cams;
+  int b;
+  __device__ __forceinline__ bool operator()(int64_t s, T pos[3], T g[C]) const {
+    const int64_t osz = p.dout.count();
+    const int slot = p.sep ? b * p.ncam + int(s / osz) : b;
+    const int64_t i = p.sep ? s % osz : s;
+    const int x = int(i % p.dout.x), y = int((i / p.dout.x) % p.dout.y), z = int(i / (int64_t(p.dout.x) * p.dout.y));
+    float q[3];
+    xf_position(cams[slot], p.cm, x + 0.5f, y + 0.5f, z + 0.5f, p.dout, p.din, q);
+    pos[0] = T(q[0]) - p.cco;
+    pos[1] = T(q[1]) - p.cco;
+    pos[2] = T(q[2]) - p.cco;
+#pragma unroll
+    for (int k = 0; k < C; ++k) g[k] = p.out_grad[(int64_t(slot) * osz + i) * C + k];
+    return true;
+  }
+};
+
 // ------------------------------------------------------------------- mips
 // One 2x2x2 level (kGenerateMip3D): pairs averaged along z, then y, then x.
 template <int C, class T>
@@ -655,6 +693,21 @@ int xf_fwd_typed(const ngt_sample_transform_args* a, cudaStream_t st) {
   return check_launch("ngt_sample_transform_fwd");
 }
 
+// Deterministic transform adjoint workspace: [per-slot cameras][gather buckets].
+size_t xf_cams_bytes(const ngt_sample_transform_args* a) {
+  const int64_t slots = a->separate_camera_batch ? a->input_shape[0] * a->num_cameras : a->input_shape[0];
+  return (size_t(slots) * sizeof(Cam) + 255) & ~size_t(255);
+}
+
+int64_t xf_det_samples(const ngt_sample_transform_args* a) {
+  return (a->separate_camera_batch ? int64_t(a->num_cameras) : 1) * a->output_dhw[0] * a->output_dhw[1] *
+         a->output_dhw[2];
+}
+
+size_t xf_det_bytes(const ngt_sample_transform_grad_args* a) {
+  return xf_cams_bytes(&a->fwd) + gather_bytes(xf_det_samples(&a->fwd), dims_of(a->fwd.input_shape), a->fwd.boundary);
+}
+
 template <class T>
 int xf_bwd_typed(const ngt_sample_transform_grad_args* a, cudaStream_t st) {
   XfParams<T> p = xf_params<T>(&a->fwd);
@@ -673,6 +726,23 @@ int xf_bwd_typed(const ngt_sample_transform_grad_args* a, cudaStream_t st) {
     if (cudaMemsetAsync(p.count, 0, need, st) != cudaSuccess) return check_launch("sample_transform_bwd memset");
   }
   const int slots = p.sep ? p.N * p.ncam : p.N;
+  if (!reference && a->deterministic) {
+    // gather form: each batch entry's samples bucketed by cell, summed per voxel in a fixed order
+    const size_t need = xf_det_bytes(a);
+    if (!a->workspace || a->workspace_bytes < need)
+      return fail(NGT_ERR_WORKSPACE, "sample_transform_bwd: deterministic mode needs %zu workspace bytes", need);
+    Cam* cams = static_cast<Cam*>(a->workspace);
+    k_xf_cams<T><<<unsigned(slots), 32, 0, st>>>(p, cams);
+    char* gw = static_cast<char*>(a->workspace) + xf_cams_bytes(&a->fwd);
+    const int64_t ns = xf_det_samples(&a->fwd);
+    for (int b = 0; b < p.N; ++b) {
+      T* ig = p.in_grad + int64_t(b) * vsz * C;
+      if (C == 1) gather_adjoint<1, T>(XfSource<1, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
+      else if (C == 2) gather_adjoint<2, T>(XfSource<2, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
+      else gather_adjoint<4, T>(XfSource<4, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
+    }
+    return check_launch("ngt_sample_transform_bwd");
+  }
   for (int s0 = 0; s0 < slots; s0 += 65535) {
     p.slot0 = s0;
     const dim3 grid(ceil_div_u(p.dout.count(), kBlock), min(65535, slots - s0));
@@ -777,7 +847,9 @@ extern "C" int ngt_sample_transform_fwd(const ngt_sample_transform_args* a, void
 }
 
 extern "C" size_t ngt_sample_transform_bwd_workspace_bytes(const ngt_sample_transform_grad_args* a) {
-  if (!a || a->grad_mode != NGT_GRAD_REFERENCE) return 0;
+  if (!a) return 0;
+  if (a->grad_mode == NGT_GRAD_EXACT && a->deterministic) return xf_det_bytes(a);
+  if (a->grad_mode != NGT_GRAD_REFERENCE) return 0;
   const int64_t* s = a->fwd.input_shape;
   return size_t(s[0] * s[1] * s[2] * s[3]) * sizeof(unsigned);
 }
@@ -794,6 +866,12 @@ extern "C" int ngt_sample_transform_bwd(const ngt_sample_transform_grad_args* a,
     return rc;
   if (a->grad_mode != NGT_GRAD_EXACT && a->grad_mode != NGT_GRAD_REFERENCE)
     return fail(NGT_ERR_INVALID_ARGUMENT, "sample_transform_bwd: invalid grad_mode");
+  if (a->deterministic && a->grad_mode == NGT_GRAD_EXACT) {
+    if (a->fwd.interpolation != NGT_LINEAR)
+      return fail(NGT_ERR_UNSUPPORTED, "sample_transform_bwd: the deterministic gather form is for LINEAR interpolation");
+    if (xf_det_samples(&a->fwd) >= (int64_t(1) << 31))
+      return fail(NGT_ERR_UNSUPPORTED, "sample_transform_bwd: the deterministic gather form takes < 2^31 samples per batch entry");
+  }
   if (a->fwd.dtype == NGT_F64) return xf_bwd_typed<double>(a, as_stream(stream));
   return xf_bwd_typed<float>(a, as_stream(stream));
 }

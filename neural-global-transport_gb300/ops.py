@@ -26,8 +26,9 @@ _DETERMINISTIC = [False]
 
 
 def set_deterministic(flag):
-    """Use the gather form (bit-reproducible) for the LUT-resample and advection
-    input gradients in exact mode."""
+    """Bit-reproducible input gradients in exact mode: the gather form for the
+    LUT and transform resamples and the advection, fixed-point integer
+    accumulation for the raymarch."""
     _DETERMINISTIC[0] = bool(flag)
 
 
@@ -109,6 +110,7 @@ def _enum(table, value, name):
 _CACHE_SIZE = 32
 _HOST_MATS = collections.OrderedDict()  # (shape, bytes, width, device) -> (tensor, event, stream)
 _CAMERAS = collections.OrderedDict()    # (ids of cached matrices, slots) -> (block, event, stream, matrices)
+_RAYS = collections.OrderedDict()       # (ids of cached matrices, slots, sizes, boundary) -> (table, event, stream, ...)
 
 
 def _cache_put(cache, key, value):
@@ -175,6 +177,35 @@ def _cameras(r, M, V, P, F):
         # the entry holds the matrices, so their ids stay theirs while it lives
         _cache_put(_CAMERAS, key, (cams,) + _recorded(cams) + ((M, V, P, F),))
     return cams
+
+
+def _rays(r, M, V, P, F):
+    """The ray table of raymarch args ``r`` (ngt_raymarch_rays: every ray set up in
+    double precision) when all four matrix buffers are cached host uploads,
+    formed once per matrices, slot layout, image and grid sizes and boundary;
+    None otherwise (the kernels then set up each ray in float arithmetic)."""
+    if any(getattr(t, "_ngt_host_key", None) is None for t in (M, V, P, F)):
+        return None
+    key = (id(M), id(V), id(P), id(F), int(r.input_shape[0]), int(r.separate_camera_batch),
+           tuple(int(v) for v in r.output_dhw), tuple(int(v) for v in r.input_shape[1:4]), int(r.boundary))
+    rays = _cache_get(_RAYS, key)
+    if rays is None:
+        lib = L.load()
+        rays = torch.empty(int(lib.ngt_raymarch_rays_bytes(ctypes.byref(r))), dtype=torch.uint8, device=M.device)
+        L.call("ngt_raymarch_rays", ctypes.byref(r), _ptr(rays), _stream())
+        _cache_put(_RAYS, key, (rays,) + _recorded(rays) + ((M, V, P, F),))
+    return rays
+
+
+def _check_matrices(input, M, V, P, F):
+    """The kernels read one model matrix per batch entry and one view, projection
+    and frustum per camera through plain pointers: shorter buffers are refused
+    here rather than read past."""
+    if M.shape[0] < input.shape[0]:
+        raise ValueError("matrix_m holds %d matrices for a batch of %d grids" % (M.shape[0], input.shape[0]))
+    if P.shape[0] < V.shape[0] or F.shape[0] < V.shape[0]:
+        raise ValueError("matrix_p / frustum_params hold fewer entries (%d / %d) than matrix_v (%d cameras)"
+                         % (P.shape[0], F.shape[0], V.shape[0]))
 
 
 def _workspace(nbytes, device):
@@ -310,21 +341,23 @@ class _SampleGridTransform(torch.autograd.Function):
         args.workspace, args.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
         L.call("ngt_sample_transform_fwd", ctypes.byref(args), _stream())
         ctx.save_for_backward(input, M, V, P, F)
-        ctx.attrs, ctx.out_dhw, ctx.mode = attrs, out_dhw, get_gradient_mode()
+        ctx.attrs, ctx.out_dhw, ctx.mode, ctx.det = attrs, out_dhw, get_gradient_mode(), get_deterministic()
         return out
 
     @staticmethod
     def backward(ctx, grad):
         input, M, V, P, F = ctx.saved_tensors
-        gi = _xf_backward(input, grad.contiguous(), M, V, P, F, ctx.out_dhw, ctx.attrs, ctx.mode)
+        gi = _xf_backward(input, grad.contiguous(), M, V, P, F, ctx.out_dhw, ctx.attrs, ctx.mode, ctx.det)
         return gi, None, None, None, None, None, None
 
 
-def _xf_backward(input, output_grad, M, V, P, F, out_dhw, a, mode):
+def _xf_backward(input, output_grad, M, V, P, F, out_dhw, a, mode, deterministic=None):
     g = L.SampleTransformGradArgs()
     g.fwd = _xf_args(input, M, V, P, F, out_dhw, None, a)
     gi = torch.empty_like(input)
     g.output_grad, g.input_grad, g.grad_mode = _ptr(output_grad), _ptr(gi), L.GRAD[mode]
+    det = get_deterministic() if deterministic is None else deterministic
+    g.deterministic = int(bool(det) and mode == "exact" and a["interpolation"] == "LINEAR")
     ws = _workspace(L.load().ngt_sample_transform_bwd_workspace_bytes(ctypes.byref(g)), input.device)
     g.workspace, g.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
     L.call("ngt_sample_transform_bwd", ctypes.byref(g), _stream())
@@ -334,8 +367,10 @@ def _xf_backward(input, output_grad, M, V, P, F, out_dhw, a, mode):
 def _xf_prepare(input, matrix_m, matrix_v, matrix_p, frustum_params):
     input = _cuda(input, "input")
     dev = input.device
-    return input, _floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev), \
-        _floats(frustum_params, 6, dev)
+    M, V, P, F = (_floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev),
+                  _floats(frustum_params, 6, dev))
+    _check_matrices(input, M, V, P, F)
+    return input, M, V, P, F
 
 
 def sample_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, output_shape, interpolation="LINEAR",
@@ -354,15 +389,17 @@ def sample_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params, o
 def sample_grid_transform_grad(input, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,
                                interpolation="LINEAR", boundary="BORDER", mipmapping="NONE", num_mipmaps=0,
                                mip_bias=0.0, coordinate_mode="TRANSFORM_LINDEPTH", cell_center_offset=0.5,
-                               separate_camera_batch=True, grad_mode=None):
-    """``SampleGridTransformGrad`` (resample_grid.cc:68-92)."""
+                               separate_camera_batch=True, grad_mode=None, deterministic=None):
+    """``SampleGridTransformGrad`` (resample_grid.cc:68-92).  ``deterministic``
+    (default: ``get_deterministic()``): the bit-reproducible gather form of the
+    exact LINEAR gradient."""
     input, M, V, P, F = _xf_prepare(input, matrix_m, matrix_v, matrix_p, frustum_params)
     output_grad = _cuda(output_grad, "output_grad").to(input.dtype)
     attrs = dict(interpolation=interpolation, boundary=boundary, mipmapping=mipmapping, num_mipmaps=num_mipmaps,
                  mip_bias=mip_bias, coordinate_mode=coordinate_mode, cell_center_offset=cell_center_offset,
                  separate_camera_batch=separate_camera_batch)
     return _xf_backward(input, output_grad, M, V, P, F, tuple(output_grad.shape[2:5]), attrs,
-                        grad_mode or get_gradient_mode())
+                        grad_mode or get_gradient_mode(), deterministic)
 
 
 def lod_transform(input_shape, matrix_mv, matrix_p, frustum_params, output_shape, inverse_transform=False,
@@ -443,6 +480,9 @@ def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
     cams = _cameras(r, M, V, P, F)
     if cams is not None:
         r.cameras = _ptr(cams)
+    rays = _rays(r, M, V, P, F)
+    if rays is not None:
+        r.rays = _ptr(rays)
     lib = L.load()
     quad = None
     if keep_quad:
@@ -457,16 +497,21 @@ def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
     return out, quad
 
 
-def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode, quad=None):
+def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode, quad=None, deterministic=None):
     g = L.RaymarchGradArgs()
     g.fwd = _ray_args(input, M, V, P, F, out_dhw, None, a)
     cams = _cameras(g.fwd, M, V, P, F)
     if cams is not None:
         g.fwd.cameras = _ptr(cams)
-    if quad is not None and mode == "exact":
+    rays = _rays(g.fwd, M, V, P, F)
+    if rays is not None:
+        g.fwd.rays = _ptr(rays)
+    det = bool(get_deterministic() if deterministic is None else deterministic) and mode == "exact"
+    if quad is not None and mode == "exact" and not det:
         g.fwd.quad = _ptr(quad)
     gi = torch.empty(input.shape, dtype=compute_dtype(input), device=input.device)
     g.output, g.output_grad, g.input_grad, g.grad_mode = _ptr(output), _ptr(output_grad), _ptr(gi), L.GRAD[mode]
+    g.deterministic = int(det)
     ws = _workspace(L.load().ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g)), input.device)
     g.workspace, g.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
     L.call("ngt_raymarch_bwd", ctypes.byref(g), _stream())
@@ -478,17 +523,18 @@ class _RaymarchGridTransform(torch.autograd.Function):
     def forward(ctx, input, M, V, P, F, out_dhw, attrs):
         mode = get_gradient_mode()
         # the quad layout built for the forward is kept for an exact backward
+        det = get_deterministic()
         out, quad = _ray_forward(input, M, V, P, F, out_dhw, attrs,
-                                 keep_quad=ctx.needs_input_grad[0] and mode == "exact")
+                                 keep_quad=ctx.needs_input_grad[0] and mode == "exact" and not det)
         ctx.save_for_backward(input, M, V, P, F, out)
-        ctx.attrs, ctx.out_dhw, ctx.mode, ctx.quad = attrs, out_dhw, mode, quad
+        ctx.attrs, ctx.out_dhw, ctx.mode, ctx.quad, ctx.det = attrs, out_dhw, mode, quad, det
         return out
 
     @staticmethod
     def backward(ctx, grad):
         input, M, V, P, F, out = ctx.saved_tensors
         gi = _ray_backward(input, out, grad.contiguous().to(out.dtype), M, V, P, F, ctx.out_dhw, ctx.attrs, ctx.mode,
-                           quad=ctx.quad)
+                           quad=ctx.quad, deterministic=ctx.det)
         ctx.quad = None
         return gi, None, None, None, None, None, None
 
@@ -507,6 +553,7 @@ def raymarch_grid_transform(input, matrix_m, matrix_v, matrix_p, frustum_params,
     dev = input.device
     M, V, P, F = (_floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev),
                   _floats(frustum_params, 6, dev))
+    _check_matrices(input, M, V, P, F)
     attrs = dict(interpolation=interpolation, boundary=boundary, blending_mode=blending_mode, keep_dims=keep_dims,
                  separate_camera_batch=separate_camera_batch,
                  emission_scale=None if emission_scale is None else tuple(float(v) for v in emission_scale))
@@ -521,9 +568,10 @@ class _RaymarchGridTransformGrad(torch.autograd.Function):
     raymarch of the incoming volume gradient; input and output get none."""
 
     @staticmethod
-    def forward(ctx, input, output, output_grad, M, V, P, F, out_dhw, attrs, mode):
+    def forward(ctx, input, output, output_grad, M, V, P, F, out_dhw, attrs, mode, deterministic):
         ctx.geom = (M, V, P, F, out_dhw, attrs, output_grad.shape)
-        return _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, attrs, mode)
+        return _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, attrs, mode,
+                             deterministic=deterministic)
 
     @staticmethod
     def backward(ctx, grad):
@@ -534,19 +582,22 @@ class _RaymarchGridTransformGrad(torch.autograd.Function):
             raise NotImplementedError("Gradient of raymach op gradient only available for ADDITIVE blending, is %s"
                                       % blend)
         gg, _ = _ray_forward(grad.contiguous(), M, V, P, F, out_dhw, dict(attrs, emission_scale=None))
-        return None, None, gg.reshape(shape), None, None, None, None, None, None, None
+        return None, None, gg.reshape(shape), None, None, None, None, None, None, None, None
 
 
 def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v, matrix_p, frustum_params,
                                  output_shape, interpolation="LINEAR", boundary="BORDER",
                                  blending_mode="BEER_LAMBERT", keep_dims=False, separate_camera_batch=True,
-                                 grad_mode=None, emission_scale=None):
+                                 grad_mode=None, emission_scale=None, deterministic=None):
     """``RaymarchGridTransformGrad`` (raymarch_grid.cc:67-92): the input gradient.
-    Differentiable w.r.t. ``output_grad`` for ADDITIVE blending (ops_loader.py:98-118)."""
+    Differentiable w.r.t. ``output_grad`` for ADDITIVE blending (ops_loader.py:98-118).
+    ``deterministic`` (default: ``get_deterministic()``): bit-reproducible exact
+    gradient (fixed-point integer accumulation)."""
     input = _cuda(input, "input")
     dev = input.device
     M, V, P, F = (_floats(matrix_m, 16, dev), _floats(matrix_v, 16, dev), _floats(matrix_p, 16, dev),
                   _floats(frustum_params, 6, dev))
+    _check_matrices(input, M, V, P, F)
     attrs = dict(interpolation=interpolation, boundary=boundary, blending_mode=blending_mode, keep_dims=keep_dims,
                  separate_camera_batch=separate_camera_batch,
                  emission_scale=None if emission_scale is None else tuple(float(v) for v in emission_scale))
@@ -554,7 +605,8 @@ def raymarch_grid_transform_grad(input, output, output_grad, matrix_m, matrix_v,
     return _RaymarchGridTransformGrad.apply(input, _cuda(output, "output").to(cd),
                                             _cuda(output_grad, "output_grad").to(cd), M, V, P, F,
                                             tuple(int(s) for s in list(output_shape)[:3]), attrs,
-                                            grad_mode or get_gradient_mode())
+                                            grad_mode or get_gradient_mode(),
+                                            get_deterministic() if deterministic is None else bool(deterministic))
 
 
 def unproject(images, matrix_m, matrix_v, matrix_p, frustum_params, grid_dhw, depth, interpolation="LINEAR",

@@ -17,6 +17,7 @@ built once; ``capture()`` records the whole step as one CUDA graph.
 """
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -122,6 +123,12 @@ class RenderAdvectStep:
         self._call("ngt_raymarch_cameras", ctypes.byref(r), _ptr(self.cameras),
                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
         r.cameras = _ptr(self.cameras)
+        # ... and so are their rays, set up in double precision
+        self.rays = torch.empty(int(self.lib.ngt_raymarch_rays_bytes(ctypes.byref(r))), dtype=torch.uint8,
+                                device=dev)
+        self._call("ngt_raymarch_rays", ctypes.byref(r), _ptr(self.rays),
+                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        r.rays = _ptr(self.rays)
         self.ray = r
         rg = L.RaymarchGradArgs()
         rg.fwd = r
@@ -137,6 +144,28 @@ class RenderAdvectStep:
 
     def _call(self, name, *args):
         L.call(name, *args)
+
+    def bind_inputs(self, rho, ux, uy, uz, targets=None):
+        """Point the step at other input tensors of the same shapes and dtype
+        (and other targets); the step's own buffers stay."""
+        self.rho, self.ux, self.uy, self.uz = rho, ux, uy, uz
+        for a in (self.adv, self.adv_g.fwd):
+            a.data, a.vel_x, a.vel_y, a.vel_z = _ptr(rho), _ptr(ux), _ptr(uy), _ptr(uz)
+        if targets is not None:
+            self.targets = targets
+
+    def bind_gradients(self, g_rho, g_ux, g_uy, g_uz):
+        """Write the next backward's gradients into these tensors."""
+        self.g_rho, self.g_ux, self.g_uy, self.g_uz = g_rho, g_ux, g_uy, g_uz
+        ag = self.adv_g
+        ag.data_grad, ag.vel_x_grad, ag.vel_y_grad, ag.vel_z_grad = _ptr(g_rho), _ptr(g_ux), _ptr(g_uy), _ptr(g_uz)
+
+    def backward(self, stream=None):
+        """The render and advection backward of the last forward (gradients into
+        the bound gradient tensors)."""
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream if stream is None else stream)
+        self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g), s)
+        self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_g), s)
 
     def forward(self, stream=None):
         """Advect, render and the image loss (its gradient included), added to
@@ -157,8 +186,7 @@ class RenderAdvectStep:
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self.loss.zero_()
         self.forward(s.value)
-        self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g), s)
-        self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_g), s)
+        self.backward(s.value)
 
     def loss_only(self):
         """Forward and loss only (e.g. finite differences); returns the loss tensor."""
@@ -189,3 +217,103 @@ class RenderAdvectStep:
 
     def gradients(self):
         return self.g_rho, self.g_ux, self.g_uy, self.g_uz
+
+
+# ------------------------------------------------------ differentiable call
+# Steps kept per (shapes, dtype, device, cameras, options): their intermediate
+# buffers (advected density, MacCormack fields, quad layout, images, workspaces)
+# are reused by every call with the same key.  A step is taken from forward to
+# backward; a forward while all kept steps of a key wait for their backward
+# makes another (up to _MAX_PLANS per key, after which the oldest is taken over
+# and its pending backward refuses to run).
+_PLANS = {}
+_MAX_PLANS = 4
+
+
+def _plan_key(rho, ux, uy, uz, M, V, P, F, image_dhw, options):
+    mats = tuple(np.ascontiguousarray(np.asarray(m, np.float32)).tobytes() for m in (M, V, P, F))
+    return (tuple(rho.shape), tuple(ux.shape), tuple(uy.shape), tuple(uz.shape), rho.dtype, str(rho.device),
+            tuple(int(v) for v in image_dhw), mats, tuple(sorted(options.items())))
+
+
+class _Plan:
+    def __init__(self, step):
+        self.step = step
+        self.busy = False
+        self.generation = 0
+
+
+def _take_plan(key, make):
+    plans = _PLANS.setdefault(key, [])
+    for pl in plans:
+        if not pl.busy:
+            return pl
+    if len(plans) < _MAX_PLANS:
+        plans.append(_Plan(make()))
+        return plans[-1]
+    pl = min(plans, key=lambda q: q.generation)  # the oldest pending forward loses its buffers
+    pl.busy = False
+    return pl
+
+
+class _RenderAdvectLoss(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, rho, ux, uy, uz, targets, plan, needs_backward):
+        st = plan.step
+        st.bind_inputs(rho, ux, uy, uz, targets)
+        st.loss.zero_()
+        st.forward()
+        plan.generation = max(pl.generation for pls in _PLANS.values() for pl in pls) + 1
+        plan.busy = bool(needs_backward)
+        ctx.plan, ctx.generation = plan, plan.generation
+        ctx.shapes = (rho, ux, uy, uz)
+        return st.loss[0].clone()
+
+    @staticmethod
+    def backward(ctx, g):
+        plan = ctx.plan
+        if plan.generation != ctx.generation or not plan.busy:
+            raise RuntimeError("render_advect_loss: the buffers of this forward were taken by a later call "
+                               "(more than %d forwards of the same step waiting for their backward)" % _MAX_PLANS)
+        st = plan.step
+        f = st.g_image.dtype
+        grads = [torch.empty(t.shape, dtype=f, device=t.device) for t in ctx.shapes]
+        st.bind_gradients(*grads)
+        st.g_image.mul_(g.to(f))  # the upstream scale enters through the image gradient
+        st.backward()
+        plan.busy = False
+        return grads[0], grads[1], grads[2], grads[3], None, None, None
+
+
+def render_advect_loss(rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
+                       clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", background=None):
+    """The reconstruction step's loss as one differentiable call: MacCormack warp
+    of ``rho`` (D, H, W, 1) by the MAC faces ``ux, uy, uz``, render of every camera
+    (Beer-Lambert, the [light*step, step] emission grid), optional background
+    composite, and 0.5 * sum of squared differences of the light channel to
+    ``targets`` (1, views, H, W, 1).  Returns the loss (a 0-d tensor);
+    differentiable w.r.t. rho and the three face grids.
+
+    The same work as ``advect.warp`` + ``ops.raymarch_grid_transform`` +
+    ``ops.image_l2_loss`` with autograd between them (data_structures.py:1690-1737,
+    renderer.py:718-827, optimization.py:478), as five library calls and one
+    autograd node instead of three nodes and their intermediate tensors: the
+    step's buffers are kept per shape and camera set and reused by later calls."""
+    dev = rho.device
+    rho, ux, uy, uz = (t.contiguous() for t in (rho, ux, uy, uz))
+    cd = torch.float64 if rho.dtype == torch.float64 else torch.float32
+    targets = torch.as_tensor(targets, device=dev).to(cd).contiguous()
+    options = dict(dt=float(dt), light=float(light), order=int(order), clamp=clamp, advect_boundary=advect_boundary,
+                   render_boundary=render_boundary, background=background is not None)
+    key = _plan_key(rho, ux, uy, uz, M, V, P, F, image_dhw, options)
+
+    def make():
+        return RenderAdvectStep(rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=dt, light=light, order=order,
+                                clamp=clamp, advect_boundary=advect_boundary, render_boundary=render_boundary,
+                                background=background)
+
+    plan = _take_plan(key, make)
+    if background is not None:
+        plan.step.background.copy_(torch.as_tensor(background, device=dev).to(cd).expand_as(plan.step.background))
+    needs = torch.is_grad_enabled() and any(t.requires_grad for t in (rho, ux, uy, uz))
+    return _RenderAdvectLoss.apply(rho, ux, uy, uz, targets, plan, needs)

