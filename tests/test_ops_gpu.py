@@ -453,8 +453,10 @@ def test_raymarch_autograd_signed_extinction_emission():
 
 def test_host_matrix_and_camera_caches():
     """Host matrices are uploaded once per content (a changed array uploads
-    again), cameras formed from cached uploads are reused, and results equal
-    the call given device matrices (cameras formed per call)."""
+    again), cameras and ray tables formed from cached uploads are reused, and
+    results match the call given device matrices (cameras formed per call, rays
+    set up per ray in float arithmetic instead of taken from the double-precision
+    table: the same images to a few float roundings)."""
     ops = ngt()
     M, V, P, F = scene_mats(vol_dhw=(10, 12, 14), cam_dhw=(10, 8, 6))
     dev = torch.device("cuda", 0)
@@ -466,17 +468,17 @@ def test_host_matrix_and_camera_caches():
     assert b is not a and not torch.equal(a, b)
     x = T((RNG.uniform(0, 1, (1, 10, 12, 14, 1)) * 0.3).astype(np.float32)).requires_grad_()
     y1 = ops.raymarch_grid_transform(x, M, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
-    n_cams = len(ops._CAMERAS)
+    n_cams, n_rays = len(ops._CAMERAS), len(ops._RAYS)
     y2 = ops.raymarch_grid_transform(x, M, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
-    assert len(ops._CAMERAS) == n_cams and torch.equal(y1, y2)
+    assert len(ops._CAMERAS) == n_cams and len(ops._RAYS) == n_rays and torch.equal(y1, y2)
     y3 = ops.raymarch_grid_transform(x, torch.as_tensor(M, device=dev), torch.as_tensor(V, device=dev),
                                      torch.as_tensor(P, device=dev), torch.as_tensor(F, device=dev), [10, 8, 6],
                                      emission_scale=(0.5, 1.0))
-    assert torch.equal(y1, y3)
+    assert rel(N(y3), N(y1)) < 1e-5
     g = T(RNG.standard_normal(tuple(y1.shape)).astype(np.float32))
     ga, = torch.autograd.grad(y1, x, g)
     gb, = torch.autograd.grad(y3, x, g)
-    assert rel(N(gb), N(ga)) < 1e-6
+    assert rel(N(gb), N(ga)) < 1e-5
     # moved to the new matrix content: a different image
     y4 = ops.raymarch_grid_transform(x, M2, V, P, F, [10, 8, 6], emission_scale=(0.5, 1.0))
     assert not torch.equal(y1, y4)
