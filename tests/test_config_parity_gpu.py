@@ -11,7 +11,9 @@ synthetic inputs of each configuration, in full:
 2. the differentiated step at 128^3 with all 5 views of 256 x 256 x 128;
 3. the checkpointed chain on the full 96 x 176 x 96 plume grid, 12 frames with
    checkpoints every 5 (two segment boundaries inside the chain);
-4. the 32 uneven scenes of seed 4 through the batched step.
+4. the 32 uneven scenes of seed 4 through the batched step;
+5. the configuration-2 step with density and velocity stored in bf16 / f16,
+   against the FP64 oracle on the unrounded inputs.
 
 Bars: LUT resample and advection forward bit for bit; transform resample,
 depth blend, raymarch images 1e-5 and every gradient 1e-4 relative L2 (the
@@ -240,3 +242,57 @@ def test_config4_seed4_batch(pool):
     assert max(img_err) < FWD_TOL
     assert abs(loss - ref_loss) <= bound
     assert max(grad_err) < GRAD_TOL
+
+
+# ------------------------------------------- 16-bit storage against FP64 oracle
+@pytest.fixture(scope="module")
+def fp64_config2(pool):
+    """The configuration-2 step of the FP64 oracle on the unrounded inputs, with
+    FP64 targets: (workload, targets, image, loss, gradients)."""
+    from ngt_gb300 import workloads
+    p, n = pool
+    w = workloads.config2()
+    d = lambda a: np.asarray(a, np.float64)
+    tgt, _, _ = parallel.render_l2(p, n, d(w.rho_target), w.depth_step, w.M, w.V, w.P, w.F, w.image_dhw)
+    tgt = np.ascontiguousarray(tgt[..., :1])
+    image, loss, grads = parallel.render_advect_step(p, n, d(w.rho), d(w.ux), d(w.uy), d(w.uz), w.M, w.V, w.P, w.F,
+                                                     tgt, w.image_dhw, w.depth_step)
+    return w, tgt, image, loss, grads
+
+
+@pytest.mark.parametrize("storage", ["bf16", "f16", "f32"])
+def test_config2_storage_error_vs_fp64_oracle(fp64_config2, storage):
+    """Density and velocity stored in 16 bits (FP32 interpolation, transmittance
+    and gradient accumulation) against the FP64 oracle on the unrounded inputs:
+    image <= 1e-2 and every gradient <= 2e-2 relative L2 (the stated bars for
+    reduced-precision storage); FP32 storage for comparison.  Also reported: the
+    gradients when the backward is given the FP64 run's MacCormack revert mask,
+    which separates the limiter's mask flips (a discontinuity: a cell whose
+    corrected value sits at the edge of its neighbours' range reverts in one
+    precision and not in the other) from the rounding of the stored values."""
+    from ngt_gb300.step import RenderAdvectStep
+    w, tgt, image, ref_loss, ref = fp64_config2
+    st = {"bf16": torch.bfloat16, "f16": torch.float16, "f32": torch.float32}[storage]
+    mk = lambda dt: RenderAdvectStep(T(w.rho, dt), T(w.ux, dt), T(w.uy, dt), T(w.uz, dt), w.M, w.V, w.P, w.F,
+                                     T(tgt, torch.float64 if dt == torch.float64 else torch.float32), w.image_dhw)
+    step = mk(st)
+    step.step()
+    torch.cuda.synchronize()
+    errs = dict(image=rel(step.image, image), grads=[rel(a, b) for a, b in zip(step.gradients(), ref)])
+    # the FP64 step's revert mask imposed on this storage's backward
+    ref64 = mk(torch.float64)
+    ref64.step()
+    torch.cuda.synchronize()
+    flips = int((step.mc_mask != ref64.mc_mask).sum())
+    step.loss.zero_()
+    step.forward()
+    step.mc_mask.copy_(ref64.mc_mask)
+    step.backward()
+    torch.cuda.synchronize()
+    errs["grads_fp64_mask"] = [rel(a, b) for a, b in zip(step.gradients(), ref)]
+    errs["mask_flips"] = flips
+    report("config2_storage_" + storage, **errs)
+    assert errs["image"] < (1e-5 if storage == "f32" else 1e-2)
+    # FP32 storage: float sample positions against the oracle's double ones, carried
+    # to the gradients by the residual (the bound of the FP32-vs-FP64 step check)
+    assert max(errs["grads"]) < (1e-3 if storage == "f32" else 2e-2)
