@@ -29,6 +29,9 @@
 #include "ngt_common.cuh"
 #include "ngt_gather.cuh"
 #include "ngt_host.cuh"
+#include "ngt_tma.cuh"
+
+#include <mutex>
 
 namespace ngt {
 namespace {
@@ -218,6 +221,44 @@ __global__ void __launch_bounds__(kBlock, (mc_narrow16<C, T, LK>() ? 8 : 0)) k_m
   mc_fwd1_at<C>(p, lk, x, y, z);
 }
 
+// Where the back-trace reads the fwd field's eight corners: global memory, or a
+// brick of it staged in shared memory (with global reads for corners outside it).
+struct GlobalFetch {
+  template <int C, class V, class S>
+  __device__ __forceinline__ void operator()(const V* g, const Tri<S>& t, const Dims& d, S v[8][C]) const {
+    tri_fetch<C>(g, t, d, v);
+  }
+};
+
+// A one-channel brick of kBrickX x kBrickY x kBrickZ values whose element (0, 0, 0)
+// is cell (ox, oy, oz) of the grid; corners outside it are read from ``g``.
+constexpr int kTileX = 32, kTileY = 8, kTileZ = 8, kHalo = 4;
+constexpr int kBrickX = kTileX + 2 * kHalo, kBrickY = kTileY + 2 * kHalo, kBrickZ = kTileZ + 2 * kHalo;
+
+struct BrickFetch {
+  const float* brick;
+  int ox, oy, oz;
+  bool ok;  // false: the brick did not arrive, every corner is read from global memory
+  template <int C, class V, class S>
+  __device__ __forceinline__ void operator()(const V* g, const Tri<S>& t, const Dims& d, S v[8][C]) const {
+    const int x0 = t.i0[0] - ox, x1 = t.i1[0] - ox, y0 = t.i0[1] - oy, y1 = t.i1[1] - oy;
+    const int z0 = t.i0[2] - oz, z1 = t.i1[2] - oz;
+    const bool in = ok && C == 1 && min(min(x0, x1), min(min(y0, y1), min(z0, z1))) >= 0 && max(x0, x1) < kBrickX &&
+                    max(y0, y1) < kBrickY && max(z0, z1) < kBrickZ;
+    if (!in) {
+      tri_fetch<C>(g, t, d, v);
+      return;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int lx = (k & 1) ? x1 : x0, ly = (k & 2) ? y1 : y0, lz = (k & 4) ? z1 : z0;
+      const bool valid = ((k & 1) ? t.ok1[0] : t.ok0[0]) && ((k & 2) ? t.ok1[1] : t.ok0[1]) &&
+                         ((k & 4) ? t.ok1[2] : t.ok0[2]);
+      v[k][0] = valid ? S(brick[(lz * kBrickY + ly) * kBrickX + lx]) : S(0);
+    }
+  }
+};
+
 template <int C, class S>
 struct McState {
   S fwd[C], back[C], corr[C], res[C];
@@ -226,9 +267,10 @@ struct McState {
 
 // With ``stored`` the MC_SMOOTH mask is read from p.mask instead of being
 // recomputed from the forward trace's corner extrema.
-template <int C, class T, class S>
+template <int C, class T, class S, class FE = GlobalFetch>
 __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x, int y, int z, const S lut[3],
-                                         McState<C, S>& s, S vb[8][C], Tri<S>& tb, bool stored = false) {
+                                         McState<C, S>& s, S vb[8][C], Tri<S>& tb, bool stored = false,
+                                         const FE& fe = FE()) {
   const S p2x = add_rn(-lut[0], S(x)), p2y = add_rn(-lut[1], S(y)), p2z = add_rn(-lut[2], S(z));
   tb = tri_setup(p2x, p2y, p2z, p.d, p.bm);
   if (p.bm == BORDER && !tb.inside) {
@@ -239,7 +281,7 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
 #pragma unroll
     for (int c = 0; c < C; ++c) s.back[c] = S(0);
   } else {
-    tri_fetch<C>(p.fwd, tb, p.d, vb);
+    fe.template operator()<C>(p.fwd, tb, p.d, vb);
   }
   S mn[C], mx[C];
   const bool recompute = p.clamp == NGT_CLAMP_MC_SMOOTH && !(stored && p.mask);
@@ -277,8 +319,9 @@ __device__ __forceinline__ void mc_state(const McParams<T>& p, int64_t i, int x,
   }
 }
 
-template <int C, class T, class LK>
-__device__ __forceinline__ void mc_fwd2_at(const McParams<T>& p, const LK& lk, int x, int y, int z) {
+template <int C, class T, class LK, class FE = GlobalFetch>
+__device__ __forceinline__ void mc_fwd2_at(const McParams<T>& p, const LK& lk, int x, int y, int z,
+                                           const FE& fe = FE()) {
   typedef CT<T> S;
   const int64_t i = flat(x, y, z, p.d);
   S lut[3];
@@ -286,7 +329,7 @@ __device__ __forceinline__ void mc_fwd2_at(const McParams<T>& p, const LK& lk, i
   McState<C, S> s;
   S vb[8][C];
   Tri<S> tb;
-  mc_state<C>(p, i, x, y, z, lut, s, vb, tb);
+  mc_state<C>(p, i, x, y, z, lut, s, vb, tb, false, fe);
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const S o = (p.clamp == NGT_CLAMP_NEGATIVE) ? fmax(s.res[c], S(0)) : s.res[c];
@@ -312,8 +355,9 @@ __device__ __forceinline__ void put_direct(S* p, S v, int accumulate) {
 // past the row's end stay in the warp (inactive) for the warp-merged scatter.
 // (x, y, z) is a cell of the grid; inactive lanes (padding, clamped onto the
 // row's last cell) take part in the warp-merged scatter only.
-template <int C, class T, class LK>
-__device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, int x, int y, int z, bool active) {
+template <int C, class T, class LK, class FE = GlobalFetch>
+__device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, int x, int y, int z, bool active,
+                                           const FE& fe = FE()) {
   typedef CT<T> S;
   const int64_t i = flat(x, y, z, p.d);
   if (p.gface[0] && active && !p.accumulate) {
@@ -349,7 +393,7 @@ __device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, i
     McState<C, S> s;
     S vb[8][C];
     Tri<S> tb;
-    mc_state<C>(p, i, x, y, z, lut, s, vb, tb, true);
+    mc_state<C>(p, i, x, y, z, lut, s, vb, tb, true, fe);
     S gback[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) {
@@ -409,6 +453,54 @@ __global__ void __launch_bounds__(kBlock, 5) k_mc_bwd1(McParams<T> p, LK lk) {
     y = min(y, p.d.y - 1);
   }
   mc_bwd1_at<C>(p, lk, x, y, z, active);
+}
+
+// ------------------------------------------- fwd-field bricks staged by TMA
+// Forward 2 and backward 1 of one-channel data read the fwd field at the
+// back-traced position idx - lookup, a few cells from the cell itself.  Here a
+// block takes a 32 x 8 x 8 tile of cells; one TMA copy brings the fwd field over
+// the tile and kHalo cells around it (a 40 x 16 x 16 brick, zeros outside the
+// grid) into shared memory, and the eight corners of every trace that stays in
+// the brick are read there -- traces of lookups of kHalo cells or more, and
+// wrapped indices, read global memory as before.  The values and the arithmetic
+// are those of the global-memory kernels, so the results are the same bits.
+// The block's wait for its brick is bounded; if it gives up, it reads global
+// memory for every corner and waits (bounded again) for the copy before it
+// leaves.
+constexpr int kBrickWaitPolls = 1 << 22;
+
+// Residency: 41 KB of brick per block leave room for five blocks per SM; forward 2
+// is held to the registers of five (51), backward 1 to those of four (64).
+template <int C, class T, class LK, int PHASE>
+__global__ void __launch_bounds__(kTileX * kTileY, PHASE == 1 ? 5 : 4)
+    k_mc_brick(McParams<T> p, LK lk, const __grid_constant__ CUtensorMap tmap) {
+  __shared__ alignas(128) float brick[kBrickZ * kBrickY * kBrickX];
+  __shared__ alignas(8) uint64_t bar;
+  const int tid = threadIdx.y * kTileX + threadIdx.x;
+  const int x0 = int(blockIdx.x) * kTileX, y0 = int(blockIdx.y) * kTileY, z0 = int(blockIdx.z) * kTileZ;
+  if (tid == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(&bar, unsigned(sizeof(brick)));
+    tma_load_3d(brick, &tmap, x0 - kHalo, y0 - kHalo, z0 - kHalo, &bar);
+  }
+  const bool ok = mbar_wait_bounded(&bar, 0, kBrickWaitPolls);
+  const BrickFetch fe{brick, x0 - kHalo, y0 - kHalo, z0 - kHalo, ok};
+  int x = x0 + int(threadIdx.x), y = y0 + int(threadIdx.y);
+  const bool row = x < p.d.x && y < p.d.y;
+  for (int k = 0; k < kTileZ; ++k) {
+    const int z = z0 + k;
+    if (z >= p.d.z) break;
+    if (PHASE == 1) {
+      if (row) mc_fwd2_at<C>(p, lk, x, y, z, fe);
+    } else {
+      // backward 1: padding lanes of a partial tile follow the row's last cell,
+      // inactive, for the warp-merged scatter
+      if (__all_sync(0xffffffffu, !row)) break;
+      mc_bwd1_at<C>(p, lk, row ? x : min(x, p.d.x - 1), row ? y : min(y, p.d.y - 1), z, row, fe);
+    }
+  }
+  if (!ok) mbar_wait_bounded(&bar, 0, kBrickWaitPolls);  // the copy may still be landing in the brick
 }
 
 // gather sources of the deterministic form: the back-trace (value gback at
@@ -677,11 +769,70 @@ int validate(const ngt_advect_args* a) {
 
 Dims cells_of(const int64_t* dhw) { return Dims{int(dhw[2]), int(dhw[1]), int(dhw[0])}; }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (null when the
+// driver does not offer it: the brick kernels are then not used).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    cudaGetLastError();  // a failed lookup leaves no error behind for the launches
+  });
+  return fn;
+}
+
+// The tensor map of a one-channel float field of grid d for the brick kernels;
+// false when the field does not qualify (a row of a multiple of 4 floats, so its
+// rows and planes start on 16 bytes; a 16-byte aligned base) or no encoder.
+bool brick_map(const float* f, const Dims& d, CUtensorMap& m) {
+  if (d.x % 4 != 0 || (reinterpret_cast<uintptr_t>(f) & 15) != 0) return false;
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t dims[3] = {cuuint64_t(d.x), cuuint64_t(d.y), cuuint64_t(d.z)};
+  const cuuint64_t strides[2] = {cuuint64_t(d.x) * 4, cuuint64_t(d.x) * d.y * 4};
+  const cuuint32_t box[3] = {kBrickX, kBrickY, kBrickZ};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  return fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(f), dims, strides, box, elem,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+dim3 brick_grid(const Dims& d) {
+  return dim3(ceil_div_u(d.x, kTileX), ceil_div_u(d.y, kTileY), ceil_div_u(d.z, kTileZ));
+}
+
+// Forward 2 / backward 1 (PHASE 1 / 2): through fwd-field bricks for one channel of
+// float or 16-bit density whose field qualifies, else the global-memory kernels.
+template <int C, class T, class LK, int PHASE>
+void launch_trace_phase(const McParams<T>& p, const LK& lk, cudaStream_t st) {
+  // (the velocity self-advection's face lookups keep the global-memory kernels)
+  if constexpr (C == 1 && !std::is_same<T, double>::value && !std::is_same<LK, FaceLookup<T>>::value) {
+    CUtensorMap m;
+    if (brick_map(p.fwd, p.d, m)) {
+      k_mc_brick<C, T, LK, PHASE><<<brick_grid(p.d), dim3(kTileX, kTileY), 0, st>>>(p, lk, m);
+      return;
+    }
+  }
+  const CellLaunch l = cell_launch(p.d);
+  if (PHASE == 1)
+    k_mc_fwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
+  else
+    k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
+}
+
 template <int C, class T, class LK>
 void launch_fwd(const McParams<T>& p, const LK& lk, cudaStream_t st) {
   const CellLaunch l = cell_launch(p.d);
   k_mc_fwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
-  if (p.order == 2) k_mc_fwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
+  if (p.order == 2) launch_trace_phase<C, T, LK, 1>(p, lk, st);
 }
 
 // bwd 1 + 2 of one warp; leaves the lookup gradient in p.glut
@@ -698,7 +849,10 @@ int launch_bwd12(McParams<T>& p, const LK& lk, cudaStream_t st) {
   }
   const unsigned nb = ceil_div_u(n, kBlock);
   const CellLaunch l = cell_launch(p.d);
-  k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
+  if (p.order == 2)
+    launch_trace_phase<C, T, LK, 2>(p, lk, st);
+  else
+    k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
   if (p.det && p.order == 2)
     gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st);
   if (p.reference && p.order == 2) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gfwd, p.buf, p.cnt, n);
@@ -741,8 +895,7 @@ int density_fwd(const ngt_advect_args* a, cudaStream_t st) {
     k_mc_fwd1<C, T, CenteredLookup<T>><<<l.grid, l.block, 0, st>>>(p, centered<T>(a));
     p.lut_out = nullptr;
     if (p.order == 2)
-      k_mc_fwd2<C, T, StoredLookup<T>><<<l.grid, l.block, 0, st>>>(
-          p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup), p.d});
+      launch_trace_phase<C, T, StoredLookup<T>, 1>(p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup), p.d}, st);
   }
   return check_launch("ngt_advect_maccormack_fwd");
 }

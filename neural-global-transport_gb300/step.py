@@ -15,6 +15,7 @@ one-channel rho' and forms both blend channels in registers; its gradient comes
 back as one channel.  All launches go through the C ABI with argument structs
 built once; ``capture()`` records the whole step as one CUDA graph.
 """
+import collections
 import ctypes
 
 import numpy as np
@@ -226,14 +227,62 @@ class RenderAdvectStep:
 # backward; a forward while all kept steps of a key wait for their backward
 # makes another (up to _MAX_PLANS per key, after which the oldest is taken over
 # and its pending backward refuses to run).
+#
+# Each step also keeps CUDA graphs of its forward and of its backward, keyed by
+# the addresses of the tensors they read and write (inputs and targets; input
+# gradients): PyTorch's caching allocator hands a training loop the same few
+# addresses again and again, so from the second call with the same addresses the
+# pass is one graph launch instead of a row of library calls.
 _PLANS = {}
 _MAX_PLANS = 4
+_GRAPHS_PER_PASS = 4
+_MATRIX_KEYS = collections.OrderedDict()  # ids of matrix objects -> (the objects, their content key)
+
+
+def _matrix_key(M, V, P, F):
+    """Content key of the camera matrices, memoised by object identity (the
+    objects are kept referenced with their entry, so their ids stay theirs)."""
+    ids = (id(M), id(V), id(P), id(F))
+    hit = _MATRIX_KEYS.get(ids)
+    if hit is not None and all(not isinstance(m, torch.Tensor) for m in (M, V, P, F)):
+        return hit[1]
+    key = tuple(np.ascontiguousarray(np.asarray(m.detach().cpu() if isinstance(m, torch.Tensor) else m,
+                                                np.float32)).tobytes() for m in (M, V, P, F))
+    _MATRIX_KEYS[ids] = ((M, V, P, F), key)
+    if len(_MATRIX_KEYS) > 64:
+        _MATRIX_KEYS.popitem(last=False)
+    return key
 
 
 def _plan_key(rho, ux, uy, uz, M, V, P, F, image_dhw, options):
-    mats = tuple(np.ascontiguousarray(np.asarray(m, np.float32)).tobytes() for m in (M, V, P, F))
     return (tuple(rho.shape), tuple(ux.shape), tuple(uy.shape), tuple(uz.shape), rho.dtype, str(rho.device),
-            tuple(int(v) for v in image_dhw), mats, tuple(sorted(options.items())))
+            tuple(int(v) for v in image_dhw), _matrix_key(M, V, P, F), tuple(sorted(options.items())))
+
+
+class _Pass:
+    """Graphs of one pass of a step, by the addresses it binds."""
+
+    def __init__(self):
+        self.graphs = collections.OrderedDict()
+        self.seen = collections.deque(maxlen=_GRAPHS_PER_PASS)
+
+    def run(self, key, body):
+        g = self.graphs.get(key)
+        if g is not None:
+            self.graphs.move_to_end(key)
+            g.replay()
+            return
+        if key not in self.seen:  # first call at these addresses: run it directly
+            self.seen.append(key)
+            body()
+            return
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            body()
+        self.graphs[key] = g
+        if len(self.graphs) > _GRAPHS_PER_PASS:
+            self.graphs.popitem(last=False)
+        g.replay()
 
 
 class _Plan:
@@ -241,6 +290,13 @@ class _Plan:
         self.step = step
         self.busy = False
         self.generation = 0
+        self.fwd = _Pass()
+        self.bwd = _Pass()
+
+    def forward(self):
+        st = self.step
+        st.loss.zero_()
+        st.forward()
 
 
 def _take_plan(key, make):
@@ -261,8 +317,8 @@ class _RenderAdvectLoss(torch.autograd.Function):
     def forward(ctx, rho, ux, uy, uz, targets, plan, needs_backward):
         st = plan.step
         st.bind_inputs(rho, ux, uy, uz, targets)
-        st.loss.zero_()
-        st.forward()
+        ctx.fwd_key = tuple(t.data_ptr() for t in (rho, ux, uy, uz, targets))
+        plan.fwd.run(ctx.fwd_key, plan.forward)
         plan.generation = max(pl.generation for pls in _PLANS.values() for pl in pls) + 1
         plan.busy = bool(needs_backward)
         ctx.plan, ctx.generation = plan, plan.generation
@@ -280,7 +336,8 @@ class _RenderAdvectLoss(torch.autograd.Function):
         grads = [torch.empty(t.shape, dtype=f, device=t.device) for t in ctx.shapes]
         st.bind_gradients(*grads)
         st.g_image.mul_(g.to(f))  # the upstream scale enters through the image gradient
-        st.backward()
+        # the advection backward also reads the forward's inputs
+        plan.bwd.run(ctx.fwd_key + tuple(t.data_ptr() for t in grads), st.backward)
         plan.busy = False
         return grads[0], grads[1], grads[2], grads[3], None, None, None
 
@@ -298,7 +355,9 @@ def render_advect_loss(rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, 
     ``ops.image_l2_loss`` with autograd between them (data_structures.py:1690-1737,
     renderer.py:718-827, optimization.py:478), as five library calls and one
     autograd node instead of three nodes and their intermediate tensors: the
-    step's buffers are kept per shape and camera set and reused by later calls."""
+    step's buffers are kept per shape and camera set and reused by later calls,
+    and its passes are replayed as CUDA graphs once the same tensor addresses
+    come back."""
     dev = rho.device
     rho, ux, uy, uz = (t.contiguous() for t in (rho, ux, uy, uz))
     cd = torch.float64 if rho.dtype == torch.float64 else torch.float32
