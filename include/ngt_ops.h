@@ -230,7 +230,9 @@ typedef struct {
    * boundary (static cameras across calls).  Those are set up in double
    * precision and rounded once, so the march starts from the float nearest the
    * exact start; null: set up per ray in float arithmetic.  Used by the forward
-   * and the exact backward. */
+   * and the exact backward.  With up to 4096 (camera, 16x8-pixel tile) items the
+   * table also holds the items ordered by their rays' summed sample counts, and
+   * the forward and the one-pass backward start the longest items first. */
   const void* rays;
 } ngt_raymarch_args;
 
@@ -281,11 +283,12 @@ int ngt_raymarch_fwd(const ngt_raymarch_args* args, void* stream);
  * ngt_raymarch_quad fails with NGT_ERR_UNSUPPORTED.  No counterpart in the
  * reference, whose kernels gather the eight corners per sample
  * (sampling_v2.hpp:37-124). */
-/* The ray table of args (32 bytes per (batch, camera) slot and pixel, 16-byte
- * aligned): the ray set-up of getRaymarchStep / RayGridIntersectionDistances
- * (raymarch_grid.cu.cc:109-200) in double precision, rounded to the float start
- * and step the march accumulates.  No counterpart in the reference, which sets
- * up every ray in float arithmetic in each kernel. */
+/* The ray table of args (32 bytes per (batch, camera) slot and pixel, then the
+ * item order; 16-byte aligned): the ray set-up of getRaymarchStep /
+ * RayGridIntersectionDistances (raymarch_grid.cu.cc:109-200) in double
+ * precision, rounded to the float start and step the march accumulates.  No
+ * counterpart in the reference, which sets up every ray in float arithmetic in
+ * each kernel. */
 size_t ngt_raymarch_rays_bytes(const ngt_raymarch_args* args);
 int ngt_raymarch_rays(const ngt_raymarch_args* args, void* rays, void* stream);
 size_t ngt_raymarch_quad_bytes(const ngt_raymarch_args* args);
@@ -365,6 +368,12 @@ typedef struct {
    * there and forward 2 and the backward read it instead of averaging the
    * faces again.  Null: averaged in every kernel.  No reference counterpart. */
   void* lookup;
+  /* Storage of the three face grids when it differs from dtype: NGT_F16 faces
+   * with NGT_BF16 data (BF16's exponent range keeps the near-empty tails of a
+   * density that the limiter compares, FP16's mantissa keeps four times finer
+   * velocities and so trace positions).  NGT_F32 (0): the faces are stored as
+   * dtype.  Single-grid calls only. */
+  int32_t velocity_dtype;
 } ngt_advect_args;
 
 typedef struct {
@@ -525,6 +534,17 @@ int ngt_version(void);
 /* sizeof of the argument struct named ``name`` (e.g. "ngt_raymarch_args"), 0 for
  * an unknown name: lets a binding check its mirror of the layouts. */
 size_t ngt_struct_size(const char* name);
+/* Bounded waits.  A kernel that waits for an asynchronous copy (the MacCormack
+ * forward's TMA-staged bricks of the fwd field) gives up after a bounded number
+ * of polls, counts the event, finishes with plain global-memory reads (the same
+ * results) and waits again, bounded, for its copy before it leaves.
+ * ngt_wait_timeouts copies the count into *count (synchronising the device) and
+ * clears it when reset is non-zero.  ngt_set_wait_polls sets the poll limit of
+ * the first wait (default 4194304; 0 makes every first wait give up at once, a
+ * way to exercise the path; negative restores the default) and returns the
+ * previous limit.  No reference counterpart (its kernels do not wait). */
+int ngt_wait_timeouts(uint64_t* count, int32_t reset);
+int32_t ngt_set_wait_polls(int32_t polls);
 
 #ifdef __cplusplus
 }

@@ -86,7 +86,7 @@ class AdvectArgs(ctypes.Structure):
     _fields_ = [("dtype", c_i32), ("grid_dhw", I64x3), ("channels", c_i32), ("data", c_vp), ("vel_x", c_vp),
                 ("vel_y", c_vp), ("vel_z", c_vp), ("dt", c_f32), ("order", c_i32), ("clamp", c_i32),
                 ("boundary", c_i32), ("output", c_vp), ("fwd_field", c_vp), ("mask", c_vp), ("extrema", c_vp),
-                ("lookup", c_vp)]
+                ("lookup", c_vp), ("velocity_dtype", c_i32)]
 
 
 class AdvectGradArgs(ctypes.Structure):
@@ -155,6 +155,8 @@ SIGNATURES = {
     "ngt_last_error_message": ([], ctypes.c_char_p),
     "ngt_version": ([], c_i32),
     "ngt_struct_size": ([ctypes.c_char_p], c_sz),
+    "ngt_wait_timeouts": ([ctypes.POINTER(ctypes.c_uint64), c_i32], c_i32),
+    "ngt_set_wait_polls": ([c_i32], c_i32),
 }
 
 _lib = None

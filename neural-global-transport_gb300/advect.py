@@ -47,7 +47,14 @@ def _args(data, vx, vy, vz, out, fwd, dt, order, clamp, boundary, mask=None, ext
     a.mask = _ptr(mask)
     a.extrema = _ptr(extrema)
     a.lookup = _ptr(lookup)
+    if vx.dtype != data.dtype:
+        a.velocity_dtype = _code(vx)  # FP16 faces with BF16 data
     return a
+
+
+def _face_dtype(data, v):
+    """The faces' storage: the data's, except FP16 faces kept with BF16 data."""
+    return v.dtype if (data.dtype == torch.bfloat16 and v.dtype == torch.float16) else data.dtype
 
 
 def _check_faces(data, vx, vy, vz):
@@ -122,15 +129,16 @@ def warp(data, vel_x, vel_y, vel_z, dt=1.0, order=2, clamp="MC_SMOOTH", boundary
     (x: D,H,W+1; y: D,H+1,W; z: D+1,H,W).  order 1 is semi-Lagrangian, order 2
     MacCormack; clamp 'MC_SMOOTH' reverts to the semi-Lagrangian value where the
     correction leaves the range of the forward lookup's corners, 'NEGATIVE'
-    clips at 0, 'NONE' does neither."""
+    clips at 0, 'NONE' does neither.  The faces are used in the data's storage
+    type, except that FP16 faces are kept as they are with BF16 data."""
     lead = data.dim() == 5
     d = _spatial(data, "data")
     vx, vy, vz = _faces(vel_x, "vel_x"), _faces(vel_y, "vel_y"), _faces(vel_z, "vel_z")
     _check_faces(d, vx, vy, vz)
     if clamp.upper() == "MC":
         raise NotImplementedError("MIM and MAX warp sampling have wrong gradients.")
-    out = _Warp.apply(d, vx.to(d.dtype), vy.to(d.dtype), vz.to(d.dtype), float(dt), int(order), clamp.upper(),
-                      boundary)
+    fd = _face_dtype(d, vx)
+    out = _Warp.apply(d, vx.to(fd), vy.to(fd), vz.to(fd), float(dt), int(order), clamp.upper(), boundary)
     return out[None] if lead else out
 
 

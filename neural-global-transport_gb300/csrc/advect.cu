@@ -31,6 +31,7 @@
 #include "ngt_host.cuh"
 #include "ngt_tma.cuh"
 
+#include <atomic>
 #include <mutex>
 
 namespace ngt {
@@ -221,8 +222,8 @@ __global__ void __launch_bounds__(kBlock, (mc_narrow16<C, T, LK>() ? 8 : 0)) k_m
   mc_fwd1_at<C>(p, lk, x, y, z);
 }
 
-// Where the back-trace reads the fwd field's eight corners: global memory, or a
-// brick of it staged in shared memory (with global reads for corners outside it).
+// Where forward 2's back-trace reads the fwd field's eight corners: global memory,
+// or a brick of it staged in shared memory (global reads for corners outside it).
 struct GlobalFetch {
   template <int C, class V, class S>
   __device__ __forceinline__ void operator()(const V* g, const Tri<S>& t, const Dims& d, S v[8][C]) const {
@@ -232,7 +233,7 @@ struct GlobalFetch {
 
 // A one-channel brick of kBrickX x kBrickY x kBrickZ values whose element (0, 0, 0)
 // is cell (ox, oy, oz) of the grid; corners outside it are read from ``g``.
-constexpr int kTileX = 32, kTileY = 8, kTileZ = 8, kHalo = 4;
+constexpr int kTileX = 32, kTileY = 8, kTileZ = 4, kHalo = 4;
 constexpr int kBrickX = kTileX + 2 * kHalo, kBrickY = kTileY + 2 * kHalo, kBrickZ = kTileZ + 2 * kHalo;
 
 struct BrickFetch {
@@ -241,20 +242,25 @@ struct BrickFetch {
   bool ok;  // false: the brick did not arrive, every corner is read from global memory
   template <int C, class V, class S>
   __device__ __forceinline__ void operator()(const V* g, const Tri<S>& t, const Dims& d, S v[8][C]) const {
-    const int x0 = t.i0[0] - ox, x1 = t.i1[0] - ox, y0 = t.i0[1] - oy, y1 = t.i1[1] - oy;
-    const int z0 = t.i0[2] - oz, z1 = t.i1[2] - oz;
-    const bool in = ok && C == 1 && min(min(x0, x1), min(min(y0, y1), min(z0, z1))) >= 0 && max(x0, x1) < kBrickX &&
-                    max(y0, y1) < kBrickY && max(z0, z1) < kBrickZ;
+    // one base element and the upper corners' offsets (0 where the boundary rule
+    // put both corners of an axis on one cell); the corners' order is tri_fetch's
+    const int x0 = t.i0[0] - ox, y0 = t.i0[1] - oy, z0 = t.i0[2] - oz;
+    const int dx = t.i1[0] - t.i0[0], dy = t.i1[1] - t.i0[1], dz = t.i1[2] - t.i0[2];
+    const bool in = ok && C == 1 && unsigned(x0) < unsigned(kBrickX - 1) && unsigned(y0) < unsigned(kBrickY - 1) &&
+                    unsigned(z0) < unsigned(kBrickZ - 1) && unsigned(dx) <= 1u && unsigned(dy) <= 1u &&
+                    unsigned(dz) <= 1u;
     if (!in) {
       tri_fetch<C>(g, t, d, v);
       return;
     }
+    const float* b = brick + (z0 * kBrickY + y0) * kBrickX + x0;
+    const int oy = dy * kBrickX, oz = dz * (kBrickX * kBrickY);
+    const float c[8] = {b[0], b[dx], b[oy], b[oy + dx], b[oz], b[oz + dx], b[oz + oy], b[oz + oy + dx]};
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      const int lx = (k & 1) ? x1 : x0, ly = (k & 2) ? y1 : y0, lz = (k & 4) ? z1 : z0;
       const bool valid = ((k & 1) ? t.ok1[0] : t.ok0[0]) && ((k & 2) ? t.ok1[1] : t.ok0[1]) &&
                          ((k & 4) ? t.ok1[2] : t.ok0[2]);
-      v[k][0] = valid ? S(brick[(lz * kBrickY + ly) * kBrickX + lx]) : S(0);
+      v[k][0] = valid ? S(c[k]) : S(0);
     }
   }
 };
@@ -355,9 +361,8 @@ __device__ __forceinline__ void put_direct(S* p, S v, int accumulate) {
 // past the row's end stay in the warp (inactive) for the warp-merged scatter.
 // (x, y, z) is a cell of the grid; inactive lanes (padding, clamped onto the
 // row's last cell) take part in the warp-merged scatter only.
-template <int C, class T, class LK, class FE = GlobalFetch>
-__device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, int x, int y, int z, bool active,
-                                           const FE& fe = FE()) {
+template <int C, class T, class LK>
+__device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, int x, int y, int z, bool active) {
   typedef CT<T> S;
   const int64_t i = flat(x, y, z, p.d);
   if (p.gface[0] && active && !p.accumulate) {
@@ -393,7 +398,7 @@ __device__ __forceinline__ void mc_bwd1_at(const McParams<T>& p, const LK& lk, i
     McState<C, S> s;
     S vb[8][C];
     Tri<S> tb;
-    mc_state<C>(p, i, x, y, z, lut, s, vb, tb, true, fe);
+    mc_state<C>(p, i, x, y, z, lut, s, vb, tb, true);
     S gback[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) {
@@ -456,24 +461,27 @@ __global__ void __launch_bounds__(kBlock, 5) k_mc_bwd1(McParams<T> p, LK lk) {
 }
 
 // ------------------------------------------- fwd-field bricks staged by TMA
-// Forward 2 and backward 1 of one-channel data read the fwd field at the
-// back-traced position idx - lookup, a few cells from the cell itself.  Here a
-// block takes a 32 x 8 x 8 tile of cells; one TMA copy brings the fwd field over
-// the tile and kHalo cells around it (a 40 x 16 x 16 brick, zeros outside the
-// grid) into shared memory, and the eight corners of every trace that stays in
-// the brick are read there -- traces of lookups of kHalo cells or more, and
-// wrapped indices, read global memory as before.  The values and the arithmetic
-// are those of the global-memory kernels, so the results are the same bits.
-// The block's wait for its brick is bounded; if it gives up, it reads global
-// memory for every corner and waits (bounded again) for the copy before it
-// leaves.
+// Forward 2 of one-channel data reads the fwd field at the back-traced position
+// idx - lookup, a few cells from the cell itself.  Here a block takes a 32 x 8 x
+// 4 tile of cells; one TMA copy brings the fwd field over the tile and kHalo
+// cells around it (a 40 x 16 x 12 brick, zeros outside the grid) into shared
+// memory, and the eight corners of every trace that stays in the brick are read
+// there -- traces of lookups of kHalo cells or more, and wrapped indices, read
+// global memory as before.  The values and the arithmetic are those of the
+// global-memory kernel, so the results are the same bits.  (Backward 1 reads the
+// same corners but measured faster from global memory: its registers leave it
+// four resident bricked blocks per SM against five unbricked.)  The block's
+// wait for its brick is bounded by ``polls``; if it gives up, it counts the event
+// in g_wait_timeouts, reads global memory for every corner and waits (bounded by
+// kBrickWaitPolls) for the copy before it leaves, so no copy outlives its block.
 constexpr int kBrickWaitPolls = 1 << 22;
+__device__ unsigned long long g_wait_timeouts;
 
-// Residency: 41 KB of brick per block leave room for five blocks per SM; forward 2
-// is held to the registers of five (51), backward 1 to those of four (64).
-template <int C, class T, class LK, int PHASE>
-__global__ void __launch_bounds__(kTileX * kTileY, PHASE == 1 ? 5 : 4)
-    k_mc_brick(McParams<T> p, LK lk, const __grid_constant__ CUtensorMap tmap) {
+// 30 KB of brick per block leave room for seven blocks per SM; the registers are
+// held to those of five (48).
+template <int C, class T, class LK>
+__global__ void __launch_bounds__(kTileX * kTileY, 5)
+    k_mc_fwd2_brick(McParams<T> p, LK lk, const __grid_constant__ CUtensorMap tmap, int polls) {
   __shared__ alignas(128) float brick[kBrickZ * kBrickY * kBrickX];
   __shared__ alignas(8) uint64_t bar;
   const int tid = threadIdx.y * kTileX + threadIdx.x;
@@ -484,20 +492,15 @@ __global__ void __launch_bounds__(kTileX * kTileY, PHASE == 1 ? 5 : 4)
     mbar_expect_tx(&bar, unsigned(sizeof(brick)));
     tma_load_3d(brick, &tmap, x0 - kHalo, y0 - kHalo, z0 - kHalo, &bar);
   }
-  const bool ok = mbar_wait_bounded(&bar, 0, kBrickWaitPolls);
+  const bool ok = mbar_wait_bounded(&bar, 0, polls);
+  if (!ok && tid == 0) atomicAdd(&g_wait_timeouts, 1ull);
   const BrickFetch fe{brick, x0 - kHalo, y0 - kHalo, z0 - kHalo, ok};
-  int x = x0 + int(threadIdx.x), y = y0 + int(threadIdx.y);
-  const bool row = x < p.d.x && y < p.d.y;
-  for (int k = 0; k < kTileZ; ++k) {
-    const int z = z0 + k;
-    if (z >= p.d.z) break;
-    if (PHASE == 1) {
-      if (row) mc_fwd2_at<C>(p, lk, x, y, z, fe);
-    } else {
-      // backward 1: padding lanes of a partial tile follow the row's last cell,
-      // inactive, for the warp-merged scatter
-      if (__all_sync(0xffffffffu, !row)) break;
-      mc_bwd1_at<C>(p, lk, row ? x : min(x, p.d.x - 1), row ? y : min(y, p.d.y - 1), z, row, fe);
+  const int x = x0 + int(threadIdx.x), y = y0 + int(threadIdx.y);
+  if (x < p.d.x && y < p.d.y) {
+    for (int k = 0; k < kTileZ; ++k) {
+      const int z = z0 + k;
+      if (z >= p.d.z) break;
+      mc_fwd2_at<C>(p, lk, x, y, z, fe);
     }
   }
   if (!ok) mbar_wait_bounded(&bar, 0, kBrickWaitPolls);  // the copy may still be landing in the brick
@@ -759,9 +762,13 @@ int validate(const ngt_advect_args* a) {
   if (!valid_channels(a->channels)) return fail(NGT_ERR_INVALID_ARGUMENT, "Only 1,2 and 4 Channel supported.");
   if (!a->data || !a->vel_x || !a->vel_y || !a->vel_z) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null pointer");
   if (a->order == 2 && !a->fwd_field) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: MacCormack needs fwd_field");
-  if ((rc = check_aligned("advect", storage_bytes(a->dtype), {{"data", a->data}, {"vel_x", a->vel_x},
-                                                              {"vel_y", a->vel_y}, {"vel_z", a->vel_z},
-                                                              {"output", a->output}})))
+  if (a->velocity_dtype != NGT_F32 && a->velocity_dtype != a->dtype &&
+      !(a->dtype == NGT_BF16 && a->velocity_dtype == NGT_F16))
+    return fail(NGT_ERR_UNSUPPORTED, "advect: faces stored apart from the data in FP16 go with BF16 data only");
+  const int vt = a->velocity_dtype == NGT_F32 ? a->dtype : a->velocity_dtype;
+  if ((rc = check_aligned("advect", storage_bytes(a->dtype), {{"data", a->data}, {"output", a->output}})) ||
+      (rc = check_aligned("advect", storage_bytes(vt), {{"vel_x", a->vel_x}, {"vel_y", a->vel_y},
+                                                        {"vel_z", a->vel_z}})))
     return rc;
   return check_aligned("advect", arith_bytes(a->dtype),
                        {{"fwd_field", a->fwd_field}, {"extrema", a->extrema}, {"lookup", a->lookup}});
@@ -809,30 +816,30 @@ dim3 brick_grid(const Dims& d) {
   return dim3(ceil_div_u(d.x, kTileX), ceil_div_u(d.y, kTileY), ceil_div_u(d.z, kTileZ));
 }
 
-// Forward 2 / backward 1 (PHASE 1 / 2): through fwd-field bricks for one channel of
-// float or 16-bit density whose field qualifies, else the global-memory kernels.
-template <int C, class T, class LK, int PHASE>
-void launch_trace_phase(const McParams<T>& p, const LK& lk, cudaStream_t st) {
-  // (the velocity self-advection's face lookups keep the global-memory kernels)
+// first-wait poll limit of the bricked kernels (ngt_set_wait_polls)
+std::atomic<int> g_wait_polls{kBrickWaitPolls};
+
+// Forward 2: through fwd-field bricks for one channel of float or 16-bit density
+// whose field qualifies, else the global-memory kernel.
+template <int C, class T, class LK>
+void launch_fwd2(const McParams<T>& p, const LK& lk, cudaStream_t st) {
+  // (the velocity self-advection's face lookups keep the global-memory kernel)
   if constexpr (C == 1 && !std::is_same<T, double>::value && !std::is_same<LK, FaceLookup<T>>::value) {
     CUtensorMap m;
     if (brick_map(p.fwd, p.d, m)) {
-      k_mc_brick<C, T, LK, PHASE><<<brick_grid(p.d), dim3(kTileX, kTileY), 0, st>>>(p, lk, m);
+      k_mc_fwd2_brick<C, T, LK><<<brick_grid(p.d), dim3(kTileX, kTileY), 0, st>>>(p, lk, m, g_wait_polls.load());
       return;
     }
   }
   const CellLaunch l = cell_launch(p.d);
-  if (PHASE == 1)
-    k_mc_fwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
-  else
-    k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
+  k_mc_fwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
 }
 
 template <int C, class T, class LK>
 void launch_fwd(const McParams<T>& p, const LK& lk, cudaStream_t st) {
   const CellLaunch l = cell_launch(p.d);
   k_mc_fwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
-  if (p.order == 2) launch_trace_phase<C, T, LK, 1>(p, lk, st);
+  if (p.order == 2) launch_fwd2<C, T, LK>(p, lk, st);
 }
 
 // bwd 1 + 2 of one warp; leaves the lookup gradient in p.glut
@@ -849,10 +856,7 @@ int launch_bwd12(McParams<T>& p, const LK& lk, cudaStream_t st) {
   }
   const unsigned nb = ceil_div_u(n, kBlock);
   const CellLaunch l = cell_launch(p.d);
-  if (p.order == 2)
-    launch_trace_phase<C, T, LK, 2>(p, lk, st);
-  else
-    k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
+  k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
   if (p.det && p.order == 2)
     gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st);
   if (p.reference && p.order == 2) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gfwd, p.buf, p.cnt, n);
@@ -877,30 +881,32 @@ McParams<T> density_params(const ngt_advect_args* a) {
   return p;
 }
 
-template <class T>
-CenteredLookup<T> centered(const ngt_advect_args* a) {
-  return CenteredLookup<T>{static_cast<const T*>(a->vel_x), static_cast<const T*>(a->vel_y),
-                           static_cast<const T*>(a->vel_z), cells_of(a->grid_dhw), a->dt};
+// The faces' lookup; V is the faces' storage type (the data's, or FP16 faces with
+// BF16 data), its arithmetic the data's (float).
+template <class V>
+CenteredLookup<V> centered(const ngt_advect_args* a) {
+  return CenteredLookup<V>{static_cast<const V*>(a->vel_x), static_cast<const V*>(a->vel_y),
+                           static_cast<const V*>(a->vel_z), cells_of(a->grid_dhw), a->dt};
 }
 
-template <int C, class T>
+template <int C, class T, class V = T>
 int density_fwd(const ngt_advect_args* a, cudaStream_t st) {
   McParams<T> p = density_params<T>(a);
   if (!a->lookup) {
-    launch_fwd<C, T>(p, centered<T>(a), st);
+    launch_fwd<C, T>(p, centered<V>(a), st);
   } else {
     // forward 1 averages the faces once and stores the lookup; forward 2 reads it
     const CellLaunch l = cell_launch(p.d);
     p.lut_out = static_cast<CT<T>*>(a->lookup);
-    k_mc_fwd1<C, T, CenteredLookup<T>><<<l.grid, l.block, 0, st>>>(p, centered<T>(a));
+    k_mc_fwd1<C, T, CenteredLookup<V>><<<l.grid, l.block, 0, st>>>(p, centered<V>(a));
     p.lut_out = nullptr;
     if (p.order == 2)
-      launch_trace_phase<C, T, StoredLookup<T>, 1>(p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup), p.d}, st);
+      launch_fwd2<C, T, StoredLookup<T>>(p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup), p.d}, st);
   }
   return check_launch("ngt_advect_maccormack_fwd");
 }
 
-template <int C, class T>
+template <int C, class T, class V = T>
 int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
   typedef CT<T> S;
   McParams<T> p = density_params<T>(&g->fwd);
@@ -934,7 +940,7 @@ int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
   }
   int rc = g->fwd.lookup
                ? launch_bwd12<C, T>(p, StoredLookup<T>{static_cast<const CT<T>*>(g->fwd.lookup), p.d}, st)
-               : launch_bwd12<C, T>(p, centered<T>(&g->fwd), st);
+               : launch_bwd12<C, T>(p, centered<V>(&g->fwd), st);
   if (rc) return rc;
   if (faces && p.det) {
     const Dims& d = p.d;
@@ -946,22 +952,27 @@ int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
   return check_launch("ngt_advect_maccormack_bwd");
 }
 
-template <class T>
+template <class T, class V = T>
 int density_fwd_c(const ngt_advect_args* a, cudaStream_t st) {
   switch (a->channels) {
-    case 1: return density_fwd<1, T>(a, st);
-    case 2: return density_fwd<2, T>(a, st);
-    default: return density_fwd<4, T>(a, st);
+    case 1: return density_fwd<1, T, V>(a, st);
+    case 2: return density_fwd<2, T, V>(a, st);
+    default: return density_fwd<4, T, V>(a, st);
   }
 }
 
-template <class T>
+template <class T, class V = T>
 int density_bwd_c(const ngt_advect_grad_args* g, cudaStream_t st) {
   switch (g->fwd.channels) {
-    case 1: return density_bwd<1, T>(g, st);
-    case 2: return density_bwd<2, T>(g, st);
-    default: return density_bwd<4, T>(g, st);
+    case 1: return density_bwd<1, T, V>(g, st);
+    case 2: return density_bwd<2, T, V>(g, st);
+    default: return density_bwd<4, T, V>(g, st);
   }
+}
+
+// FP16 faces with BF16 data: the one mixed storage the density warp takes.
+bool mixed_faces(const ngt_advect_args* a) {
+  return a->velocity_dtype != NGT_F32 && a->velocity_dtype != a->dtype;
 }
 
 // ----------------------------------------------------------- velocity warp
@@ -1115,6 +1126,7 @@ int validate_batch(const ngt_advect_args* const* a, int count, int& zsum, int& m
     if (!a[i]->output) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null output");
     if (a[i]->dtype != a[0]->dtype || a[i]->channels != a[0]->channels)
       return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: grids must share dtype and channels");
+    if (mixed_faces(a[i])) return fail(NGT_ERR_UNSUPPORTED, "advect batch: faces in the data's storage type");
     blocks += ((a[i]->grid_dhw[2] + 31) / 32) * ((a[i]->grid_dhw[1] + 7) / 8) * a[i]->grid_dhw[0];
   }
   if (blocks >= (int64_t(1) << 31)) return fail(NGT_ERR_INVALID_ARGUMENT, "advect batch: grids too large");
@@ -1220,11 +1232,28 @@ int batch_bwd_c(const ngt_advect_grad_args* g, int count, int zsum, int mw, int 
 
 using namespace ngt;
 
+extern "C" int ngt_wait_timeouts(uint64_t* count, int32_t reset) {
+  if (!count) return fail(NGT_ERR_INVALID_ARGUMENT, "ngt_wait_timeouts: count is null");
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_wait_timeouts, sizeof(v)) != cudaSuccess) return check_launch("ngt_wait_timeouts");
+  if (reset) {
+    const unsigned long long zero = 0;
+    if (cudaMemcpyToSymbol(g_wait_timeouts, &zero, sizeof(zero)) != cudaSuccess) return check_launch("ngt_wait_timeouts");
+  }
+  *count = uint64_t(v);
+  return NGT_OK;
+}
+
+extern "C" int32_t ngt_set_wait_polls(int32_t polls) {
+  return g_wait_polls.exchange(polls < 0 ? kBrickWaitPolls : int(polls));
+}
+
 extern "C" int ngt_advect_maccormack_fwd(const ngt_advect_args* a, void* stream) {
   int rc = validate(a);
   if (rc) return rc;
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "advect: null output");
   cudaStream_t st = as_stream(stream);
+  if (mixed_faces(a)) return density_fwd_c<__nv_bfloat16, __half>(a, st);
   switch (a->dtype) {
     case NGT_F32: return density_fwd_c<float>(a, st);
     case NGT_F64: return density_fwd_c<double>(a, st);
@@ -1264,6 +1293,7 @@ extern "C" int ngt_advect_maccormack_bwd(const ngt_advect_grad_args* g, void* st
   if (!g->workspace || g->workspace_bytes < need)
     return fail(NGT_ERR_WORKSPACE, "advect_bwd needs %zu workspace bytes", need);
   cudaStream_t st = as_stream(stream);
+  if (mixed_faces(&g->fwd)) return density_bwd_c<__nv_bfloat16, __half>(g, st);
   switch (g->fwd.dtype) {
     case NGT_F32: return density_bwd_c<float>(g, st);
     case NGT_F64: return density_bwd_c<double>(g, st);

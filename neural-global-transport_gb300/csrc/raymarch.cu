@@ -25,6 +25,9 @@ namespace ngt {
 namespace {
 using namespace rm;
 
+// The largest number of (slot, tile) items a ray table orders (one block sorts them).
+constexpr int kMaxOrdered = 4096;
+
 // A slot's inverse projection and inverse model-view in double, formed by the
 // 32 lanes of a warp (lanes 0-15 one element of MV^-1, 16-31 one of P^-1).
 struct CamD {
@@ -136,6 +139,58 @@ __global__ void k_build_rays(const __grid_constant__ RayParams p, float4* __rest
   o[1] = make_float4(float(st[0]), float(st[1]), float(st[2]), hit ? 1.0f : 0.0f);
 }
 
+// The summed sample counts of the rays of every (slot, tile) item, one block each.
+__global__ void k_tile_cost(const __grid_constant__ RayParams p, const float4* __restrict__ rays, int tiles,
+                            int* __restrict__ cost) {
+  const int item = int(blockIdx.x);
+  const int slot = item / tiles, tile = item - slot * tiles;
+  int px, py;
+  pixel_of_thread(px, py);
+  const int tiles_x = (p.W + kTileX - 1) / kTileX;
+  px += (tile % tiles_x) * kTileX;
+  py += (tile / tiles_x) * kTileY;
+  int n = 0;
+  if (px < p.W && py < p.H) {
+    const float4* q = rays + 2 * ((int64_t(slot) * p.H + py) * p.W + px);
+    n = q[1].w != 0.0f ? __float_as_int(q[0].w) : 0;
+  }
+  __shared__ int part[kThreads / 32];
+  int v = n;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kThreads / 32; ++w) t += part[w];
+    cost[item] = t;
+  }
+}
+
+// ``order`` = the n <= kMaxOrdered items by descending cost (ties by item), one
+// block sorting (cost, item) keys bitonically in shared memory.
+__global__ void __launch_bounds__(1024) k_tile_order(const int* __restrict__ cost, int n, int* __restrict__ order) {
+  __shared__ unsigned long long key[kMaxOrdered];
+  for (int i = threadIdx.x; i < kMaxOrdered; i += blockDim.x)
+    key[i] = i < n ? ((unsigned long long)(0x7fffffff - cost[i]) << 32) | unsigned(i) : ~0ull;
+  __syncthreads();
+  for (int k = 2; k <= kMaxOrdered; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < kMaxOrdered; i += blockDim.x) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = key[i], b = key[l];
+          if ((a > b) == ((i & k) == 0)) {
+            key[i] = b;
+            key[l] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) order[i] = int(key[i] & 0xffffffffu);
+}
+
 // Every (batch, camera) slot's camera, one warp per slot, formed once per call
 // into ``cams`` for the raymarch blocks to copy.
 __global__ void k_build_cams(RayParams p, Cam* __restrict__ cams) {
@@ -237,6 +292,7 @@ RayParams make_params(const ngt_raymarch_args* a) {
   p.blend = a->blending_mode;
   for (int i = 0; i < 4; ++i) p.scale[i] = a->emission_scale[i];
   p.rays = static_cast<const float4*>(a->rays);
+  p.order = nullptr;
   return p;
 }
 
@@ -445,13 +501,43 @@ void build_cams(RayParams& p, const ngt_raymarch_args* a, void* at, cudaStream_t
   p.cams = cams;
 }
 
+size_t rays_table_bytes(const ngt_raymarch_args* a) {
+  return align256(size_t(slots_of(a) * a->output_dhw[1] * a->output_dhw[2]) * 2 * sizeof(float4));
+}
+
+int64_t ray_items(const ngt_raymarch_args* a) {
+  return slots_of(a) * int64_t(ceil_div_u(a->output_dhw[2], kTileX)) * ceil_div_u(a->output_dhw[1], kTileY);
+}
+
+// The item order behind a prepared ray table (ngt_raymarch_rays), or null when
+// there are too many items to order.
+const int* ray_order(const ngt_raymarch_args* a) {
+  if (!a->rays || ray_items(a) > kMaxOrdered) return nullptr;
+  return reinterpret_cast<const int*>(static_cast<const char*>(a->rays) + rays_table_bytes(a));
+}
+
 int launch_slots(int dtype, int which, int cin, int cb, int tiles, cudaStream_t st, RayParams& p) {
   const int slots = num_slots(p);
+  const int* order = p.order;
+  p.order = nullptr;
+  if (order && (which == FWD || which == BWD_BL)) {
+    // the prepared order: the items with the longest rays dispatched first
+    p.order = order;
+    p.tiles = tiles;
+    p.slot0 = 0;
+    const int rc = launch_dtype(dtype, which, cin, cb, dim3(unsigned(tiles * slots)), st, p);
+    p.order = order;
+    return rc;
+  }
   for (int s0 = 0; s0 < slots; s0 += 65535) {
     p.slot0 = s0;
     const int rc = launch_dtype(dtype, which, cin, cb, dim3(tiles, min(65535, slots - s0)), st, p);
-    if (rc) return rc;
+    if (rc) {
+      p.order = order;
+      return rc;
+    }
   }
+  p.order = order;
   return NGT_OK;
 }
 
@@ -473,7 +559,10 @@ extern "C" int ngt_raymarch_cameras(const ngt_raymarch_args* a, void* cameras, v
 }
 
 extern "C" size_t ngt_raymarch_rays_bytes(const ngt_raymarch_args* a) {
-  return a ? align256(size_t(slots_of(a) * a->output_dhw[1] * a->output_dhw[2]) * 2 * sizeof(float4)) : 0;
+  if (!a) return 0;
+  const size_t n = size_t(ray_items(a));
+  // [ray table][item order][item costs]
+  return rays_table_bytes(a) + (n <= size_t(kMaxOrdered) ? 2 * align256(n * sizeof(int)) : 0);
 }
 
 extern "C" int ngt_raymarch_rays(const ngt_raymarch_args* a, void* rays, void* stream) {
@@ -488,6 +577,13 @@ extern "C" int ngt_raymarch_rays(const ngt_raymarch_args* a, void* rays, void* s
   for (int s0 = 0; s0 < slots; s0 += 65535) {
     p.slot0 = s0;
     k_build_rays<<<dim3(tiles, min(65535, slots - s0)), kThreads, 0, as_stream(stream)>>>(p, static_cast<float4*>(rays));
+  }
+  const int64_t n = ray_items(a);
+  if (n <= kMaxOrdered) {
+    int* order = reinterpret_cast<int*>(static_cast<char*>(rays) + rays_table_bytes(a));
+    int* cost = reinterpret_cast<int*>(reinterpret_cast<char*>(order) + align256(size_t(n) * sizeof(int)));
+    k_tile_cost<<<unsigned(n), kThreads, 0, as_stream(stream)>>>(p, static_cast<const float4*>(rays), tiles, cost);
+    k_tile_order<<<1, 1024, 0, as_stream(stream)>>>(cost, int(n), order);
   }
   return check_launch("ngt_raymarch_rays");
 }
@@ -530,6 +626,7 @@ int raymarch_fwd(const ngt_raymarch_args* a, const void* l2_target, int l2_lc, v
   if (rc) return rc;
   if (!a->output) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch: null output");
   RayParams p = make_params(a);
+  p.order = ray_order(a);
   if ((rc = check_prepared_quad(a))) return rc;
   p.l2_target = l2_target;
   p.l2_lc = l2_lc;
@@ -627,6 +724,7 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   if (!a->workspace || a->workspace_bytes < l.total)
     return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: needs %zu workspace bytes", l.total);
   RayParams p = make_params(&a->fwd);
+  p.order = ray_order(&a->fwd);
   p.out_fwd = a->output;
   p.out_grad = a->output_grad;
   p.in_grad = a->input_grad;

@@ -52,6 +52,11 @@ struct RayParams {
   const Cam* cams;       // per-slot cameras formed by k_build_cams, or null (each block forms its own)
   const void* quad;      // quad layout of the input (one channel, LINEAR) or null
   const float4* rays;    // per-ray start, step and sample count (ngt_raymarch_rays) or null
+  // with a ray table: the (slot, tile) items in descending order of their rays'
+  // sample counts, block b of a 1-D launch taking item order[b]; null: block
+  // (tile, slot) = (blockIdx.x, slot0 + blockIdx.y)
+  const int* order;
+  int tiles;             // tiles per slot
   float4* gquad;         // quad gradient accumulator (exact backward) or null
   QuadDims qd;
   // forward with the image L2 loss fused: per-pixel target (l2_lc channels),
@@ -196,6 +201,18 @@ __device__ __forceinline__ void slot_to_bc(const RayParams& p, int slot, int& b,
 }
 
 __host__ __device__ __forceinline__ int num_slots_dev(const RayParams& p) { return p.sep ? p.N * p.ncam : p.N; }
+
+// The (slot, tile) item of this block.
+__device__ __forceinline__ void block_item(const RayParams& p, int& slot, int& tile) {
+  if (p.order) {
+    const int it = __ldg(p.order + blockIdx.x);
+    slot = it / p.tiles;
+    tile = it - slot * p.tiles;
+  } else {
+    slot = p.slot0 + int(blockIdx.y);
+    tile = int(blockIdx.x);
+  }
+}
 
 // This thread's pixel within its 16x8 tile: each warp covers 8x4 pixels (rays
 // that stay close in the grid, so a warp's gathers share cache lines); warps 0
@@ -518,11 +535,12 @@ template <int CIN, int CB, class T, class S, int RAYS>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_fwd(RayParams p) {
   __shared__ Cam cam;
   __shared__ CamScratch cam_sh;
-  int b, c, oslot;
-  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
+  int b, c, oslot, slot, tile;
+  block_item(p, slot, tile);
+  slot_to_bc(p, slot, b, c, oslot);
+  load_cam(p, slot, b, c, cam, cam_sh);
   __syncthreads();
-  const S l = fwd_tile<CIN, CB, T, S, RAYS>(p, cam, b, oslot, blockIdx.x);
+  const S l = fwd_tile<CIN, CB, T, S, RAYS>(p, cam, b, oslot, tile);
   if (p.l2_loss) l2_block_add<S>(l, static_cast<S*>(p.l2_loss));
 }
 
@@ -745,14 +763,15 @@ template <int CIN, int CB, class T, class S, int RAYS>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(const __grid_constant__ RayParams p) {
   __shared__ Cam cam;
   __shared__ CamScratch cam_sh;
-  int b, c, oslot;
-  slot_to_bc(p, p.slot0 + blockIdx.y, b, c, oslot);
-  load_cam(p, p.slot0 + blockIdx.y, b, c, cam, cam_sh);
+  int b, c, oslot, slot, tile;
+  block_item(p, slot, tile);
+  slot_to_bc(p, slot, b, c, oslot);
+  load_cam(p, slot, b, c, cam, cam_sh);
   __syncthreads();
   if (*p.flag != 0)
-    bwd_exact_tile_call<CIN, CB, T, S, RAYS>(p, cam, b, oslot, blockIdx.x);
+    bwd_exact_tile_call<CIN, CB, T, S, RAYS>(p, cam, b, oslot, tile);
   else
-    bwd_bl_tile<CIN, CB, T, S, SC_ATOMIC, RAYS>(p, cam, b, oslot, blockIdx.x);
+    bwd_bl_tile<CIN, CB, T, S, SC_ATOMIC, RAYS>(p, cam, b, oslot, tile);
 }
 
 // The deterministic passes of the exact Beer-Lambert backward (statistics, then

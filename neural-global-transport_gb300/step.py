@@ -73,6 +73,8 @@ class RenderAdvectStep:
 
         a = L.AdvectArgs()
         a.dtype = _code(rho)
+        if self.ux.dtype != rho.dtype:  # FP16 faces with BF16 density
+            a.velocity_dtype = _code(self.ux)
         a.grid_dhw = L.I64x3(D, H, W)
         a.channels = 1
         a.data, a.vel_x, a.vel_y, a.vel_z = _ptr(self.rho), _ptr(self.ux), _ptr(self.uy), _ptr(self.uz)
@@ -255,7 +257,7 @@ def _matrix_key(M, V, P, F):
 
 
 def _plan_key(rho, ux, uy, uz, M, V, P, F, image_dhw, options):
-    return (tuple(rho.shape), tuple(ux.shape), tuple(uy.shape), tuple(uz.shape), rho.dtype, str(rho.device),
+    return (tuple(rho.shape), tuple(ux.shape), tuple(uy.shape), tuple(uz.shape), rho.dtype, ux.dtype, str(rho.device),
             tuple(int(v) for v in image_dhw), _matrix_key(M, V, P, F), tuple(sorted(options.items())))
 
 

@@ -385,3 +385,34 @@ def test_background_validation(lib):
     assert fn(ctypes.byref(r), ok, ok, 1, ok, ok, None) == L.NGT_ERR_UNSUPPORTED  # not Beer-Lambert
     r.blending_mode, r.emission_channels = 0, 0
     assert fn(ctypes.byref(r), ok, ok, 1, ok, ok, None) == L.NGT_ERR_INVALID_ARGUMENT  # one blend channel
+
+
+def test_face_storage_validation(lib):
+    """FP16 faces go with BF16 density only; other differing face types are refused."""
+    from ngt_gb300 import _lib as L
+    a = L.AdvectArgs()
+    a.grid_dhw = L.I64x3(4, 4, 4)
+    a.channels = 1
+    for f in ("data", "vel_x", "vel_y", "vel_z", "output", "fwd_field"):
+        setattr(a, f, ctypes.c_void_p(0x1000))
+    a.order, a.clamp, a.boundary = 2, 1, 1
+    a.dtype, a.velocity_dtype = L.F32, L.F16
+    assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), None) == L.NGT_ERR_UNSUPPORTED
+    a.dtype, a.velocity_dtype = L.BF16, L.F64
+    assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), None) == L.NGT_ERR_UNSUPPORTED
+    a.dtype, a.velocity_dtype = L.BF16, L.F16
+    a.vel_x = ctypes.c_void_p(0x1001)  # misaligned for 2-byte faces
+    assert lib.ngt_advect_maccormack_fwd(ctypes.byref(a), None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"vel_x" in lib.ngt_last_error_message()
+
+
+def test_wait_poll_limit_setting(lib):
+    """The bricked kernels' first-wait poll limit: the setter returns the
+    previous value and a negative value restores the default (host only)."""
+    default = lib.ngt_set_wait_polls(7)
+    assert default == 1 << 22
+    assert lib.ngt_set_wait_polls(0) == 7
+    assert lib.ngt_set_wait_polls(-1) == 0
+    assert lib.ngt_set_wait_polls(default) == default
+    from ngt_gb300 import _lib as L
+    assert lib.ngt_wait_timeouts(None, 0) == L.NGT_ERR_INVALID_ARGUMENT

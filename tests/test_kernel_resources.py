@@ -55,13 +55,15 @@ def find(reports, *parts, source=None):
     return hits[0]
 
 
-STORAGE = {"f32": "f", "bf16": "13__nv_bfloat16", "f16": "6__half"}
+# storage type of the density, and of the lookup's faces (the same type: "IfE" or,
+# for 16-bit types, the substitution "IS2_E")
+STORAGE = {"f32": ("f", "IfE"), "bf16": ("13__nv_bfloat16", "IS2_E"), "f16": ("6__half", "IS2_E")}
 
 
 @pytest.mark.parametrize("storage", sorted(STORAGE))
 def test_maccormack_register_budgets(reports, storage):
-    t = STORAGE[storage]
-    regs, st, ld = find(reports, "k_mc_fwd1ILi1E" + t + "NS0_14CenteredLookup")
+    t, faces = STORAGE[storage]
+    regs, st, ld = find(reports, "k_mc_fwd1ILi1E" + t + "NS0_14CenteredLookup" + faces)
     assert regs <= 32 and st == ld == 0
     regs, st, ld = find(reports, "k_mc_bwd2ILi1E" + t + "NS0_12StoredLookup")
     assert regs <= 48 and st == ld == 0

@@ -888,3 +888,25 @@ def test_unproject_and_its_gradient(mode):
     (vol * T(wv)).sum().backward()
     want = oops.raymarch_grid_transform(wv, M, V, P, F, [10, 8, 6], "LINEAR", "BORDER", "ADDITIVE")
     assert rel(want, N(it.grad)) < 2e-5
+
+
+def test_bf16_density_with_f16_faces():
+    """FP16 faces with BF16 density: the warp and its gradients equal the BF16
+    warp given the FP16 faces' values widened to FP32 lookups -- checked against
+    the FP64 oracle on the stored values (the storage types only round the
+    inputs; arithmetic is FP32)."""
+    from ngt_gb300 import advect, workloads
+    w = workloads.render_step(grid=(20, 24, 28), views=1, image=(8, 8), depth=8, max_u=2.0)
+    rho = torch.as_tensor(w.rho, device="cuda").to(torch.bfloat16)
+    u = [torch.as_tensor(a, device="cuda").to(torch.float16) for a in (w.ux, w.uy, w.uz)]
+    ts = [rho.requires_grad_()] + [t.requires_grad_() for t in u]
+    out = advect.warp(*ts, dt=1.0, order=2, clamp="MC_SMOOTH", boundary="CLAMP")
+    assert out.dtype == torch.bfloat16
+    g = torch.as_tensor(RNG.standard_normal(w.rho.shape).astype(np.float32), device="cuda")
+    out.float().backward(g)
+    r64 = [N(t.detach().double()) for t in ts]
+    want = oadvect.density_maccormack(*r64)
+    assert rel(want, N(out.float())) < 1e-2
+    gw = oadvect.density_maccormack_grad(*r64, N(g).astype(np.float64))
+    for t, b in zip(ts, gw):
+        assert rel(b, N(t.grad.float())) < 2e-2
