@@ -234,6 +234,17 @@ typedef struct {
    * table also holds the items ordered by their rays' summed sample counts, and
    * the forward and the one-pass backward start the longest items first. */
   const void* rays;
+  /* Optional, with a prepared quad layout and a ray table: nonzero reserves in
+   * the quad buffer (ngt_raymarch_quad_bytes grows by (batch, camera) slots x
+   * 16x8-pixel tiles x 128 rays x D' floats) room for every ray's first D'
+   * density samples.  A Beer-Lambert forward with emission through that buffer
+   * stores them (a warp's 32 rays interleaved: 128 contiguous bytes per step)
+   * and tags the buffer with its ray table; the one-pass exact backward of the
+   * same quad buffer and ray table reads them instead of gathering each
+   * sample's corners again.  ngt_raymarch_quad clears the tag.  The samples
+   * are the forward's own values, so the gradient is unchanged.  0: the
+   * backward gathers. */
+  int32_t sample_cache;
 } ngt_raymarch_args;
 
 typedef struct {

@@ -63,7 +63,8 @@ class RaymarchArgs(ctypes.Structure):
                 ("num_cameras", c_i32), ("output", c_vp), ("interpolation", c_i32), ("boundary", c_i32),
                 ("blending_mode", c_i32), ("keep_dims", c_i32), ("separate_camera_batch", c_i32),
                 ("emission_channels", c_i32), ("emission_scale", c_f32 * 4), ("workspace", c_vp),
-                ("workspace_bytes", c_sz), ("cameras", c_vp), ("quad", c_vp), ("rays", c_vp)]
+                ("workspace_bytes", c_sz), ("cameras", c_vp), ("quad", c_vp), ("rays", c_vp),
+                ("sample_cache", c_i32)]
 
 
 class RaymarchGradArgs(ctypes.Structure):

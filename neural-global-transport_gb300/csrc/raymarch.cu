@@ -409,8 +409,31 @@ bool needs_sign_flag(const ngt_raymarch_grad_args* a) {
   return a->grad_mode == NGT_GRAD_EXACT && a->fwd.blending_mode == NGT_BEER_LAMBERT && cb > 1;
 }
 
-// A prepared quad layout: [extinction-sign word, 256 bytes][quad input].
+// A prepared quad layout: [header, 256 bytes: extinction-sign word at 0, sample
+// tag at 8][quad input][cached samples, with sample_cache].
 constexpr size_t kQuadHeader = 256;
+constexpr size_t kSampleTagOffset = 8;
+
+// Cached samples of a prepared quad layout: every (slot, tile) item's 4 warps
+// hold D x 32 floats (sample_slot).
+size_t samples_bytes(const ngt_raymarch_args* a) {
+  if (!a->sample_cache) return 0;
+  const int64_t tiles = int64_t(ceil_div_u(a->output_dhw[2], kTileX)) * ceil_div_u(a->output_dhw[1], kTileY);
+  return align256(size_t(slots_of(a) * tiles * kThreads * a->output_dhw[0]) * sizeof(float));
+}
+
+// Points p at the sample cache of the prepared layout ``a->quad`` when this
+// call can keep or use it: one-channel Beer-Lambert with emission through a
+// prepared layout sized with sample_cache, and a ray table (whose address tags
+// the cache: a forward of other rays overwrites the tag).
+void use_sample_cache(const ngt_raymarch_args* a, int cb, RayParams& p) {
+  if (!a->quad || !a->sample_cache || !a->rays || !quad_case(a) || a->blending_mode != NGT_BEER_LAMBERT || cb < 2)
+    return;
+  char* q = const_cast<char*>(static_cast<const char*>(a->quad));
+  p.samples = reinterpret_cast<float*>(q + kQuadHeader + quad_bytes(a));
+  p.sample_word = reinterpret_cast<unsigned long long*>(q + kSampleTagOffset);
+  p.sample_tag = static_cast<unsigned long long>(reinterpret_cast<uintptr_t>(a->rays)) | 1ull;
+}
 
 int check_prepared_quad(const ngt_raymarch_args* a) {
   if (a->quad && !quad_case(a))
@@ -589,7 +612,7 @@ extern "C" int ngt_raymarch_rays(const ngt_raymarch_args* a, void* rays, void* s
 }
 
 extern "C" size_t ngt_raymarch_quad_bytes(const ngt_raymarch_args* a) {
-  return a && quad_case(a) ? kQuadHeader + quad_bytes(a) : 0;
+  return a && quad_case(a) ? kQuadHeader + quad_bytes(a) + samples_bytes(a) : 0;
 }
 
 extern "C" int ngt_raymarch_quad(const ngt_raymarch_args* a, void* quad, void* stream) {
@@ -603,7 +626,9 @@ extern "C" int ngt_raymarch_quad(const ngt_raymarch_args* a, void* quad, void* s
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_quad: null or not 256-byte aligned output");
   cudaStream_t st = as_stream(stream);
   char* q = static_cast<char*>(quad);
-  if (cudaMemsetAsync(q, 0, sizeof(int), st) != cudaSuccess) return check_launch("raymarch_quad memset");
+  // the sign word and the sample tag
+  if (cudaMemsetAsync(q, 0, kSampleTagOffset + sizeof(unsigned long long), st) != cudaSuccess)
+    return check_launch("raymarch_quad memset");
   const float scale = cb > 1 ? a->emission_scale[cb - 1] : 1.0f;
   const int r = build_quad(a, q + kQuadHeader, st, reinterpret_cast<int*>(q), scale);
   if (r) return r;
@@ -638,6 +663,7 @@ int raymarch_fwd(const ngt_raymarch_args* a, const void* l2_target, int l2_lc, v
   if (a->quad) {
     p.quad = static_cast<const char*>(a->quad) + kQuadHeader;
     p.qd = QuadDims::of(p.din);
+    use_sample_cache(a, cb, p);
   }
   if (a->workspace) {
     const Layout l = fwd_layout(a);
@@ -777,6 +803,7 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
     if (quad) {
       if (prepared) {
         p.quad = static_cast<const char*>(a->fwd.quad) + kQuadHeader;
+        if (bl) use_sample_cache(&a->fwd, cb, p);
       } else {
         // one channel: the quad build also checks the sign of scale * density
         rc = build_quad(&a->fwd, w + l.quad, st, bl ? reinterpret_cast<int*>(w + l.flag) : nullptr,

@@ -73,6 +73,13 @@ struct RayParams {
   unsigned long long* fix;
   struct FixStats* fst;
   int64_t nrays;
+  // sample cache (ngt_raymarch_args::sample_cache): every ray's first D density
+  // samples, stored by the Beer-Lambert forward and read by the one-pass
+  // backward when the tag word holds ``sample_tag`` (the forward writes it);
+  // null: not kept
+  float* samples;
+  unsigned long long* sample_word;
+  unsigned long long sample_tag;
 };
 
 // Deterministic exact backward.  Float atomics add the samples' contributions in
@@ -221,6 +228,14 @@ __device__ __forceinline__ void pixel_of_thread(int& px, int& py) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   px = (warp & 1) * 8 + (lane & 7);
   py = (warp >> 1) * 4 + (lane >> 3);
+}
+
+// This thread's first cached sample: warp w of tile t of slot s owns D x 32
+// floats, sample i of lane l at i * 32 + l.
+__device__ __forceinline__ int64_t sample_slot(const RayParams& p, int slot, int tile) {
+  const int tiles = ((p.W + kTileX - 1) / kTileX) * ((p.H + kTileY - 1) / kTileY);
+  return ((int64_t(slot) * tiles + tile) * (kThreads / 32) + (threadIdx.x >> 5)) * int64_t(p.D) * 32 +
+         (threadIdx.x & 31);
 }
 
 struct Ray {
@@ -494,10 +509,13 @@ __device__ __forceinline__ S fwd_tile(const RayParams& p, const Cam& cam, int b,
       float dd = 0.0f, L[CB - 1];
 #pragma unroll
       for (int k = 0; k < CB - 1; ++k) L[k] = 0.0f;
+      float* sv = RAYS != RAYS_SETUP && p.samples ? p.samples + sample_slot(p, oslot, tile) : nullptr;
+      const int ns = sv ? min(r.steps, p.D) : 0;
       for (int i = 0; i < r.steps; ++i) {
         QuadPos qp;
         float v;
         quad_sample_fma<T>(q, pos[0] - 0.5f, pos[1] - 0.5f, pos[2] - 0.5f, p.din, p.qd, p.bm, qp, v);
+        if (i < ns) sv[int64_t(i) * 32] = v;
         dd = fmaxf(dd + sc[CB - 1] * v, 0.0f);
         const float t = __expf(-dd);
 #pragma unroll
@@ -542,6 +560,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_fwd(RayParams
   __syncthreads();
   const S l = fwd_tile<CIN, CB, T, S, RAYS>(p, cam, b, oslot, tile);
   if (p.l2_loss) l2_block_add<S>(l, static_cast<S*>(p.l2_loss));
+  if (p.samples && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *p.sample_word = p.sample_tag;
 }
 
 // ------------------------------------------------------- exact backward
@@ -714,10 +733,22 @@ __device__ __forceinline__ void bwd_bl_tile(const RayParams& p, const Cam& cam, 
       const float sl = p.scale[CB - 1];
       float dd = 0.0f, w = 0.0f;
       float pos[3] = {r.s[0], r.s[1], r.s[2]};
+      // the forward's samples of these rays, when it kept them (a cache is tagged
+      // with a ray table, so the instance that sets its rays up has none)
+      const float* sv = RAYS != RAYS_SETUP && p.samples && *p.sample_word == p.sample_tag
+                            ? p.samples + sample_slot(p, oslot, tile)
+                            : nullptr;
+      const int ns = sv ? min(r.steps, p.D) : 0;
       for (int i = 0; i < r.steps; ++i) {
         QuadPos qp;
         float v;
-        const bool in = quad_sample_fma<T>(q, pos[0] - 0.5f, pos[1] - 0.5f, pos[2] - 0.5f, p.din, p.qd, p.bm, qp, v);
+        bool in;
+        if (i < ns) {
+          in = quad_setup(pos[0] - 0.5f, pos[1] - 0.5f, pos[2] - 0.5f, p.din, p.qd, p.bm, qp);
+          v = __ldcs(sv + int64_t(i) * 32);
+        } else {
+          in = quad_sample_fma<T>(q, pos[0] - 0.5f, pos[1] - 0.5f, pos[2] - 0.5f, p.din, p.qd, p.bm, qp, v);
+        }
         dd = dd + sl * v;
         const float t = __expf(-dd);
         // d rho = sum_c scale_c * t * gL_c + scale_sigma * (gD - (L.gL - W))

@@ -473,7 +473,9 @@ def _ray_out_shape(input, V, out_dhw, a):
 def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
     """The forward raymarch: (output, quad).  With ``keep_quad`` an input the
     quad gather layout serves is prepared into a buffer of its own, returned as
-    ``quad`` for the backward to reuse instead of building it again; otherwise
+    ``quad`` = (buffer, sample_cache) for the backward to reuse instead of
+    building it again; with a ray table the buffer also keeps the forward's
+    density samples (``sample_cache`` 1) for the one-pass adjoint.  Otherwise
     ``quad`` is None."""
     out = torch.empty(_ray_out_shape(input, V, out_dhw, a), dtype=compute_dtype(input), device=input.device)
     r = _ray_args(input, M, V, P, F, out_dhw, out, a)
@@ -486,11 +488,13 @@ def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
     lib = L.load()
     quad = None
     if keep_quad:
+        r.sample_cache = int(rays is not None)
         nq = int(lib.ngt_raymarch_quad_bytes(ctypes.byref(r)))
         if nq:
-            quad = torch.empty(nq, dtype=torch.uint8, device=input.device)
-            L.call("ngt_raymarch_quad", ctypes.byref(r), _ptr(quad), _stream())
-            r.quad = _ptr(quad)
+            buf = torch.empty(nq, dtype=torch.uint8, device=input.device)
+            L.call("ngt_raymarch_quad", ctypes.byref(r), _ptr(buf), _stream())
+            r.quad = _ptr(buf)
+            quad = (buf, r.sample_cache)
     ws = _workspace(lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r)), input.device)
     r.workspace, r.workspace_bytes = _ptr(ws), 0 if ws is None else ws.numel()
     L.call("ngt_raymarch_fwd", ctypes.byref(r), _stream())
@@ -508,7 +512,7 @@ def _ray_backward(input, output, output_grad, M, V, P, F, out_dhw, a, mode, quad
         g.fwd.rays = _ptr(rays)
     det = bool(get_deterministic() if deterministic is None else deterministic) and mode == "exact"
     if quad is not None and mode == "exact" and not det:
-        g.fwd.quad = _ptr(quad)
+        g.fwd.quad, g.fwd.sample_cache = _ptr(quad[0]), quad[1]
     gi = torch.empty(input.shape, dtype=compute_dtype(input), device=input.device)
     g.output, g.output_grad, g.input_grad, g.grad_mode = _ptr(output), _ptr(output_grad), _ptr(gi), L.GRAD[mode]
     g.deterministic = int(det)

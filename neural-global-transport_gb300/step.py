@@ -112,7 +112,10 @@ class RenderAdvectStep:
         r.emission_channels = 2
         r.emission_scale[0], r.emission_scale[1] = self.emission
         # the advected density in the quad gather layout, prepared once per step for
-        # the render's forward and backward
+        # the render's forward and backward; with the exact backward it also keeps
+        # the forward's density samples, which the one-pass adjoint reads back
+        # instead of gathering them again
+        r.sample_cache = 1 if grad_mode == "exact" else 0
         nq = int(self.lib.ngt_raymarch_quad_bytes(ctypes.byref(r)))
         self.ray_quad = torch.empty(nq, dtype=torch.uint8, device=dev) if nq else None
         if nq:
