@@ -158,14 +158,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-# DRAM bytes (read + write) per call of the dominant library call, summed over its
-# kernels, from one ncu capture of this workload in f32 (cold cache per kernel):
-# profiles/step_f32_128cube_5views_kernels.md
-NCU_TRAFFIC_F32 = {"raymarch_bwd": 108.2e6}
-# The resource that does bound that call's main kernel (k_raymarch_bwd_bl), from the
-# same capture: L1TEX throughput, driven by its quad gathers and vector atomics.
-NCU_LIMITER_F32 = {"raymarch_bwd": {"resource": "L1TEX (quad gathers + float4 atomics)", "pct_of_peak": 80.2,
-                                    "source": "ncu sections, profiles/step_f32_128cube_5views_kernels.md"}}
+# DRAM bytes (read + write) per call of the step's dominant library call in f32,
+# summed over the call's kernels, each kernel captured alone by ncu (one launch,
+# cold cache) on this workload.  They come from a profile, not from the run that
+# prints them; the capture and its date go with the number.
+NCU_TRAFFIC_F32 = {
+    "raymarch_bwd": {"bytes": 90.93e6 + 2.73e6 + 34.10e6,
+                     "kernels": {"k_raymarch_bwd_bl": 93.66e6, "k_quad_fold": 34.10e6},
+                     "kind": "profile", "captured": "2026-12-04",
+                     "profile": "profiles/render_backward_f32_128cube_5views.md"},
+}
+# The resources that bound that call's main kernel (k_raymarch_bwd_bl), from the same
+# capture: L1-to-L2 requests and the L2's atomic unit (its two float4 atomics per sample).
+NCU_LIMITER_F32 = {"raymarch_bwd": {"resource": "L1-to-L2 requests / L2 atomics (float4 quad-gradient atomics)",
+                                    "l1tex2xbar_req_pct": 61.3, "l2_atomic_input_pct": 44.0, "l1tex_pct": 71.1,
+                                    "captured": "2026-12-04",
+                                    "profile": "profiles/render_backward_f32_128cube_5views.md"}}
 
 
 def measured_peak_hbm():
@@ -333,12 +341,17 @@ def gpu_arm(args, world, rank, local):
     peak, peak_kind = measured_peak_hbm()
     line["hbm_frac_of_step"] = line["algorithmic_bytes_per_step"] / (ms_per_step * 1e-3) / (peak * 1e9)
     if kernel:
-        name, avg_ms, nbytes = kernel
+        name, avg_ms, nbytes, calls = kernel
+        line["call_ms"] = calls  # every library call of the step, CUDA events, L2 flushed before each step
         achieved = nbytes / (avg_ms * 1e-3) / 1e9
         line["roofline"] = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_kind": peak_kind,
-                            "traffic": NCU_TRAFFIC_F32.get(name) if args.dtype == "f32" else None,
+                            "traffic": NCU_TRAFFIC_F32[name]["bytes"] if args.dtype == "f32" and name in NCU_TRAFFIC_F32
+                            else None,
                             "algorithmic_bytes_per_launch": nbytes, "avg_ms": avg_ms}
+        if args.dtype == "f32" and name in NCU_TRAFFIC_F32:
+            t = NCU_TRAFFIC_F32[name]
+            line["roofline"]["traffic_source"] = {k: t[k] for k in ("kind", "captured", "profile", "kernels")}
         if args.dtype == "f32" and name in NCU_LIMITER_F32:
             line["roofline"]["measured_limiter"] = NCU_LIMITER_F32[name]
     if clk:
@@ -374,16 +387,16 @@ def kernel_stats(step, torch, dev, w, st, iters, flush):
     nbytes = {
         "advect_fwd": es * (2 * n_rho + n_u),                 # rho, u read; rho' written
         "raymarch_quad": es * n_rho,                          # rho' read (its gather layout is scratch)
-        "raymarch_fwd_l2": es * n_rho + 4 * (2 * px + px + 2 * px),  # rho' read; image, target, image grad
-        "raymarch_bwd": es * n_rho + 4 * (2 * px * 2) + 4 * n_rho,  # rho', image, grad read; d rho' written
+        # rho' read; image and image gradient written, target read; d rho' written
+        "raymarch_fwd_l2_bwd": es * n_rho + 4 * (2 * px + px + 2 * px) + 4 * n_rho,
         "advect_bwd": es * (n_rho + n_u) + 4 * (n_rho + n_rho) + 4 * (n_rho + n_u),  # rho,u,fwd,grad in; grads out
     }
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    # the step's library calls, in its order
     calls = [("advect_fwd", lambda: step._call("ngt_advect_maccormack_fwd", ctypes.byref(step.adv), s)),
              ("raymarch_quad", lambda: step._call("ngt_raymarch_quad", ctypes.byref(step.ray), _ptr(step.ray_quad), s)),
-             ("raymarch_fwd_l2", lambda: step._call("ngt_raymarch_fwd_l2", ctypes.byref(step.ray), _ptr(step.targets), 1,
-                                                    _ptr(step.g_image), _ptr(step.loss), s)),
-             ("raymarch_bwd", lambda: step._call("ngt_raymarch_bwd", ctypes.byref(step.ray_g), s)),
+             ("raymarch_fwd_l2_bwd", lambda: step._call("ngt_raymarch_fwd_l2_bwd", ctypes.byref(step.ray_g), None,
+                                                        _ptr(step.targets), 1, _ptr(step.loss), s)),
              ("advect_bwd", lambda: step._call("ngt_advect_maccormack_bwd", ctypes.byref(step.adv_g), s))]
     tot = {n: 0.0 for n, _ in calls}
     for it in range(iters + 2):
@@ -400,7 +413,7 @@ def kernel_stats(step, torch, dev, w, st, iters, flush):
             for n, a, b in evs:
                 tot[n] += a.elapsed_time(b)
     name = max(tot, key=tot.get)
-    return name, tot[name] / iters, nbytes[name]
+    return name, tot[name] / iters, nbytes[name], {n: tot[n] / iters for n in tot}
 
 
 def e2e_measure(torch, dev, w, st, tgt, args, flush, fused=True):

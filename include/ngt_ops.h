@@ -306,6 +306,21 @@ size_t ngt_raymarch_quad_bytes(const ngt_raymarch_args* args);
 int ngt_raymarch_quad(const ngt_raymarch_args* args, void* quad, void* stream);
 int ngt_raymarch_bwd(const ngt_raymarch_grad_args* args, void* stream);
 size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args* args);
+/* A render's forward, its image L2 loss and its backward in one call:
+ * ngt_raymarch_fwd_l2 (or ngt_raymarch_fwd_l2_background with a non-null
+ * ``background``) writing the image to args->output and the loss gradient to
+ * args->output_grad (both written here), then ngt_raymarch_bwd of that gradient
+ * into args->input_grad.  For the exact float-atomic Beer-Lambert adjoint with
+ * emission of a one-channel LINEAR input in float or 16-bit storage this is one
+ * launch: the loss gradient of a pixel depends on that pixel alone, so each
+ * thread marches its ray forward and back in turn, the image is not read back,
+ * and the samples cached on the way (sample_cache) are read by the same
+ * thread.  Other settings run the two passes (args->fwd.workspace then serves
+ * the forward).  Workspace and other fields as ngt_raymarch_bwd.  No reference
+ * counterpart: the renderer runs the op, the loss and the registered gradient
+ * as three TF ops (renderer.py:718-827, optimization.py:478). */
+int ngt_raymarch_fwd_l2_bwd(const ngt_raymarch_grad_args* args, const void* background, const void* target,
+                            int32_t loss_channels, void* loss, void* stream);
 /* ngt_raymarch_bwd for callers that cannot allocate device memory -- a host
  * program whose own pool owns the whole device, or a loop that may not allocate
  * once it runs.  No counterpart in the reference.  args->workspace is ignored:

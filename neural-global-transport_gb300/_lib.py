@@ -135,6 +135,7 @@ SIGNATURES = {
     "ngt_background_composite_bwd": ([c_i32, c_i64, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp], c_i32),
     "ngt_raymarch_fwd": ([ctypes.POINTER(RaymarchArgs), c_vp], c_i32),
     "ngt_raymarch_bwd": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
+    "ngt_raymarch_fwd_l2_bwd": ([ctypes.POINTER(RaymarchGradArgs), c_vp, c_vp, c_i32, c_vp, c_vp], c_i32),
     "ngt_raymarch_bwd_workspace_bytes": ([ctypes.POINTER(RaymarchGradArgs)], c_sz),
     "ngt_raymarch_bwd_static": ([ctypes.POINTER(RaymarchGradArgs), c_vp], c_i32),
     "ngt_raymarch_batch_workspace_bytes": ([ctypes.POINTER(RaymarchArgs), c_i32], c_sz),

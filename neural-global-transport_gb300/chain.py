@@ -126,6 +126,7 @@ class AdvectRenderChain:
             r.blending_mode, r.keep_dims, r.separate_camera_batch = L.BLEND["BEER_LAMBERT"], 0, 1
             r.emission_channels = 2
             r.emission_scale[0], r.emission_scale[1] = light * depth_step, depth_step
+            r.sample_cache = 1  # the render backward reads its forward's samples
             return r
 
         self.ray = [ray_args(self.seg[j + 1]) for j in range(K)]
@@ -174,13 +175,6 @@ class AdvectRenderChain:
     def _call(self, name, *args):
         L.call(name, *args)
 
-    def _render_loss(self, j, t, s):
-        """Frame t's render (segment slot j) with its image loss and gradient."""
-        if self.ray_quad is not None:
-            self._call("ngt_raymarch_quad", ctypes.byref(self.ray[j]), _ptr(self.ray_quad), s)
-        self._call("ngt_raymarch_fwd_l2", ctypes.byref(self.ray[j]), _ptr(self.targets[t]), 1, _ptr(self.g_image),
-                   _ptr(self.loss), s)
-
     # ------------------------------------------------------------------ the chain
     def launch(self):
         """Enqueue forward (checkpoints) and backward on the current stream."""
@@ -211,8 +205,11 @@ class AdvectRenderChain:
                 self.seg[j + 1].add_(self.source)
             for j in range(s1 - s0 - 1, -1, -1):
                 t = s0 + j
-                self._render_loss(j, t, s)
-                self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g[(j, k)]), s)  # g_rho[k] += render grad
+                # frame t's render, image loss and render backward in one launch: g_rho[k] += render grad
+                if self.ray_quad is not None:
+                    self._call("ngt_raymarch_quad", ctypes.byref(self.ray[j]), _ptr(self.ray_quad), s)
+                self._call("ngt_raymarch_fwd_l2_bwd", ctypes.byref(self.ray_g[(j, k)]), None, _ptr(self.targets[t]), 1,
+                           _ptr(self.loss), s)
                 self.g_rho[1 - k].zero_()
                 self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_bwd[(j, k)]), s)  # and g_u +=
                 k = 1 - k

@@ -543,7 +543,7 @@ int launch_slots(int dtype, int which, int cin, int cb, int tiles, cudaStream_t 
   const int slots = num_slots(p);
   const int* order = p.order;
   p.order = nullptr;
-  if (order && (which == FWD || which == BWD_BL)) {
+  if (order && (which == FWD || which == BWD_BL || which == FWD_L2_BWD)) {
     // the prepared order: the items with the longest rays dispatched first
     p.order = order;
     p.tiles = tiles;
@@ -727,8 +727,67 @@ extern "C" size_t ngt_raymarch_bwd_workspace_bytes(const ngt_raymarch_grad_args*
   return a ? bwd_layout(a).total : 0;
 }
 
+namespace {
+// The image L2 loss of a render fused with its forward and backward
+// (ngt_raymarch_fwd_l2_bwd); null for a plain backward.
+struct FusedLoss {
+  const void* target;
+  int lc;
+  void* loss;
+  const void* background;
+};
+
+// Whether the fused call runs as one launch (k_raymarch_fwd_bwd): the exact,
+// float-atomic Beer-Lambert adjoint with emission through the quad layout.
+bool fused_launch(const ngt_raymarch_grad_args* a) {
+  return a->grad_mode == NGT_GRAD_EXACT && !a->deterministic && quad_case(&a->fwd) && needs_sign_flag(a);
+}
+
+int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void* stream);
+}  // namespace
+
 extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_bwd: null arguments");
+  return raymarch_bwd_impl(a, nullptr, stream);
+}
+
+extern "C" int ngt_raymarch_fwd_l2_bwd(const ngt_raymarch_grad_args* a, const void* background, const void* target,
+                                       int32_t loss_channels, void* loss, void* stream) {
+  if (!a) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd: null arguments");
+  if (!target || !loss || !a->output || !a->output_grad)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd: null pointer");
+  int cin, cb;
+  int rc = validate(&a->fwd, cin, cb);
+  if (rc) return rc;
+  if ((rc = check_aligned("raymarch_fwd_l2_bwd", arith_bytes(a->fwd.dtype),
+                          {{"target", target}, {"loss", loss}, {"background", background}})))
+    return rc;
+  if (background) {
+    if (cb < 2)
+      return fail(NGT_ERR_INVALID_ARGUMENT,
+                  "raymarch_fwd_l2_bwd: the background needs light channels and an optical depth channel");
+    if (a->fwd.blending_mode != NGT_BEER_LAMBERT)
+      return fail(NGT_ERR_UNSUPPORTED, "raymarch_fwd_l2_bwd: the transmittance exp(-d) is Beer-Lambert's");
+  }
+  const int top = background ? cb - 1 : cb;
+  if (loss_channels <= 0 || loss_channels > top)
+    return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd: loss_channels must be in 1..%d", top);
+  const FusedLoss fl = {target, int(loss_channels), loss, background};
+  if (!fused_launch(a)) {
+    // the two passes: the forward with its loss, then the backward
+    ngt_raymarch_args f = a->fwd;
+    f.output = const_cast<void*>(a->output);
+    void* ig = const_cast<void*>(a->output_grad);
+    rc = background ? ngt_raymarch_fwd_l2_background(&f, background, target, loss_channels, ig, loss, stream)
+                    : ngt_raymarch_fwd_l2(&f, target, loss_channels, ig, loss, stream);
+    if (rc) return rc;
+    return raymarch_bwd_impl(a, nullptr, stream);
+  }
+  return raymarch_bwd_impl(a, &fl, stream);
+}
+
+namespace {
+int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void* stream) {
   int cin, cb;
   int rc = validate(&a->fwd, cin, cb);
   if (rc) return rc;
@@ -823,7 +882,19 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
         rc = launch_dtype(a->fwd.dtype, SIGN, cin, cb, dim3(1), st, p);
         if (rc) return rc;
       }
-      rc = launch_slots(a->fwd.dtype, BWD_BL, cin, cb, tiles, st, p);  // one-pass, or checkpointed on the flag
+      if (fl) {
+        // forward, loss and backward in one launch (fused_launch): the image and its
+        // loss gradient are written to output and output_grad
+        p.output = const_cast<void*>(a->output);
+        p.l2_target = fl->target;
+        p.l2_lc = fl->lc;
+        p.l2_grad = const_cast<void*>(a->output_grad);
+        p.l2_loss = fl->loss;
+        p.l2_bkg = fl->background;
+        rc = launch_slots(a->fwd.dtype, FWD_L2_BWD, cin, cb, tiles, st, p);
+      } else {
+        rc = launch_slots(a->fwd.dtype, BWD_BL, cin, cb, tiles, st, p);  // one-pass, or checkpointed on the flag
+      }
       if (rc) return rc;
     } else {
       rc = launch_slots(a->fwd.dtype, BWD_EXACT, cin, cb, tiles, st, p);
@@ -865,6 +936,7 @@ extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
   }
   return check_launch("ngt_raymarch_bwd");
 }
+}  // namespace
 
 // ------------------------------------------------------------ batched calls
 namespace ngt {

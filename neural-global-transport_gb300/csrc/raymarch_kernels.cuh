@@ -124,7 +124,7 @@ struct RayBatch {
 };
 
 enum Which { FWD = 0, BWD_EXACT = 1, BWD_REF = 2, BWD_BL = 3, SIGN = 4, BWD_EXACT_MAX = 5, BWD_EXACT_FIX = 6,
-             BWD_BL_MAX = 7, BWD_BL_FIX = 8 };
+             BWD_BL_MAX = 7, BWD_BL_FIX = 8, FWD_L2_BWD = 9 };
 
 
 // Launch one pass of the single-scene kernels (``which``) for the storage type in
@@ -703,9 +703,11 @@ __global__ void __launch_bounds__(kThreads) k_raymarch_bwd_exact(RayParams p) {
 // output.  One march replaces the checkpointed recomputation; the sign of the
 // extinction channel is checked over the whole grid first (k_extinction_sign),
 // and a launch that can see a negative sample runs k_raymarch_bwd_exact.
+// ``fresh``: this thread has just run the forward of its ray (the fused launch),
+// so the samples it cached are there whatever the tag word says.
 template <int CIN, int CB, class T, class S, int MODE = SC_ATOMIC, int RAYS = RAYS_ANY>
 __device__ __forceinline__ void bwd_bl_tile(const RayParams& p, const Cam& cam, int b, int oslot, int tile,
-                                            FixAcc* fa = nullptr, int fe = 0) {
+                                            FixAcc* fa = nullptr, int fe = 0, bool fresh = false) {
   int px, py;
   if (!tile_pixel(p, tile, px, py)) return;
   const T* g = reinterpret_cast<const T*>(p.input) + int64_t(b) * p.din.count() * CIN;
@@ -735,7 +737,7 @@ __device__ __forceinline__ void bwd_bl_tile(const RayParams& p, const Cam& cam, 
       float pos[3] = {r.s[0], r.s[1], r.s[2]};
       // the forward's samples of these rays, when it kept them (a cache is tagged
       // with a ray table, so the instance that sets its rays up has none)
-      const float* sv = RAYS != RAYS_SETUP && p.samples && *p.sample_word == p.sample_tag
+      const float* sv = RAYS != RAYS_SETUP && p.samples && (fresh || *p.sample_word == p.sample_tag)
                             ? p.samples + sample_slot(p, oslot, tile)
                             : nullptr;
       const int ns = sv ? min(r.steps, p.D) : 0;
@@ -803,6 +805,31 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_raymarch_bwd_bl(const 
     bwd_exact_tile_call<CIN, CB, T, S, RAYS>(p, cam, b, oslot, tile);
   else
     bwd_bl_tile<CIN, CB, T, S, SC_ATOMIC, RAYS>(p, cam, b, oslot, tile);
+}
+
+// Forward, image L2 loss and one-pass backward of every ray in one launch.  The
+// loss gradient of a pixel depends on that pixel's output alone, so the thread
+// that marched a ray forward (writing its image pixel and loss gradient, and
+// caching its samples) marches it again for the adjoint, reading back what it
+// wrote: no other block's results are needed, and the image and its gradient
+// are not read back by a second launch.  Launches with a possibly negative
+// extinction sample take the checkpointed adjoint after the forward.
+template <int CIN, int CB, class T, class S, int RAYS>
+__global__ void __launch_bounds__(kThreads, 8) k_raymarch_fwd_bwd(const __grid_constant__ RayParams p) {
+  __shared__ Cam cam;
+  __shared__ CamScratch cam_sh;
+  int b, c, oslot, slot, tile;
+  block_item(p, slot, tile);
+  slot_to_bc(p, slot, b, c, oslot);
+  load_cam(p, slot, b, c, cam, cam_sh);
+  __syncthreads();
+  const S l = fwd_tile<CIN, CB, T, S, RAYS>(p, cam, b, oslot, tile);
+  l2_block_add<S>(l, static_cast<S*>(p.l2_loss));
+  if (p.samples && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *p.sample_word = p.sample_tag;
+  if (*p.flag != 0)
+    bwd_exact_tile_call<CIN, CB, T, S, RAYS>(p, cam, b, oslot, tile);
+  else
+    bwd_bl_tile<CIN, CB, T, S, SC_ATOMIC, RAYS>(p, cam, b, oslot, tile, nullptr, 0, true);
 }
 
 // The deterministic passes of the exact Beer-Lambert backward (statistics, then
@@ -945,6 +972,13 @@ void launch(int which, dim3 grid, cudaStream_t st, const RayParams& p) {
         k_raymarch_bwd_bl<CIN, CB, T, S, RAYS_TABLE><<<grid, kThreads, 0, st>>>(p);
       else
         k_raymarch_bwd_bl<CIN, CB, T, S, RAYS_SETUP><<<grid, kThreads, 0, st>>>(p);
+    }
+  } else if (which == FWD_L2_BWD) {
+    if constexpr (CB > 1) {
+      if (p.rays)
+        k_raymarch_fwd_bwd<CIN, CB, T, S, RAYS_TABLE><<<grid, kThreads, 0, st>>>(p);
+      else
+        k_raymarch_fwd_bwd<CIN, CB, T, S, RAYS_SETUP><<<grid, kThreads, 0, st>>>(p);
     }
   } else if (which == BWD_EXACT_MAX) {
     k_raymarch_bwd_exact<CIN, CB, T, S, SC_MAX><<<grid, kThreads, 0, st>>>(p);

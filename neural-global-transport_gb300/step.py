@@ -27,11 +27,11 @@ from .ops import _code, _ptr
 
 class RenderAdvectStep:
     # kernels of one f32 exact Beer-Lambert step: advect fwd 2, the quad layout of
-    # the advected density with its extinction-sign check (shared by the render's
-    # forward and backward) 1, raymarch fwd with the image loss in its epilogue 1,
-    # raymarch bwd 2 (the one-pass march -- checkpointed where the sign check
-    # fails -- and the fold), advect bwd 2
-    KERNELS_PER_STEP = 8
+    # the advected density with its extinction-sign check 1, the render's forward,
+    # image loss and backward in one launch 1 (each ray marched forward and back;
+    # the checkpointed adjoint where the sign check fails), the quad-gradient fold
+    # 1, advect bwd 2
+    KERNELS_PER_STEP = 7
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact",
@@ -166,21 +166,28 @@ class RenderAdvectStep:
         ag = self.adv_g
         ag.data_grad, ag.vel_x_grad, ag.vel_y_grad, ag.vel_z_grad = _ptr(g_rho), _ptr(g_ux), _ptr(g_uy), _ptr(g_uz)
 
-    def backward(self, stream=None):
+    def backward(self, stream=None, render=True):
         """The render and advection backward of the last forward (gradients into
-        the bound gradient tensors)."""
+        the bound gradient tensors); ``render`` False: the advection backward
+        only, after a forward that ran the render's backward with it."""
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream if stream is None else stream)
-        self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g), s)
+        if render:
+            self._call("ngt_raymarch_bwd", ctypes.byref(self.ray_g), s)
         self._call("ngt_advect_maccormack_bwd", ctypes.byref(self.adv_g), s)
 
-    def forward(self, stream=None):
+    def forward(self, stream=None, render_backward=False):
         """Advect, render and the image loss (its gradient included), added to
-        ``self.loss``."""
+        ``self.loss``; with ``render_backward`` the render's backward too (into the
+        advected density's gradient), in the same launch as its forward."""
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream if stream is None else stream)
         self._call("ngt_advect_maccormack_fwd", ctypes.byref(self.adv), s)
         if self.ray_quad is not None:
             self._call("ngt_raymarch_quad", ctypes.byref(self.ray), _ptr(self.ray_quad), s)
-        if self.background is None:
+        if render_backward:
+            bkg = None if self.background is None else _ptr(self.background)
+            self._call("ngt_raymarch_fwd_l2_bwd", ctypes.byref(self.ray_g), bkg, _ptr(self.targets), 1,
+                       _ptr(self.loss), s)
+        elif self.background is None:
             self._call("ngt_raymarch_fwd_l2", ctypes.byref(self.ray), _ptr(self.targets), 1, _ptr(self.g_image),
                        _ptr(self.loss), s)
         else:
@@ -191,8 +198,8 @@ class RenderAdvectStep:
         """Enqueue forward + loss + backward on the current stream."""
         s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self.loss.zero_()
-        self.forward(s.value)
-        self.backward(s.value)
+        self.forward(s.value, render_backward=True)
+        self.backward(s.value, render=False)
 
     def loss_only(self):
         """Forward and loss only (e.g. finite differences); returns the loss tensor."""
@@ -298,10 +305,10 @@ class _Plan:
         self.fwd = _Pass()
         self.bwd = _Pass()
 
-    def forward(self):
+    def forward(self, render_backward=False):
         st = self.step
         st.loss.zero_()
-        st.forward()
+        st.forward(render_backward=render_backward)
 
 
 def _take_plan(key, make):
@@ -323,7 +330,10 @@ class _RenderAdvectLoss(torch.autograd.Function):
         st = plan.step
         st.bind_inputs(rho, ux, uy, uz, targets)
         ctx.fwd_key = tuple(t.data_ptr() for t in (rho, ux, uy, uz, targets))
-        plan.fwd.run(ctx.fwd_key, plan.forward)
+        # a forward whose backward will follow runs the render's backward with it
+        # (one launch); the advection backward waits for the upstream gradient
+        nb = bool(needs_backward)
+        plan.fwd.run(ctx.fwd_key + (nb,), lambda: plan.forward(render_backward=nb))
         plan.generation = max(pl.generation for pls in _PLANS.values() for pl in pls) + 1
         plan.busy = bool(needs_backward)
         ctx.plan, ctx.generation = plan, plan.generation
@@ -340,9 +350,10 @@ class _RenderAdvectLoss(torch.autograd.Function):
         f = st.g_image.dtype
         grads = [torch.empty(t.shape, dtype=f, device=t.device) for t in ctx.shapes]
         st.bind_gradients(*grads)
-        st.g_image.mul_(g.to(f))  # the upstream scale enters through the image gradient
+        # the render's gradient (linear in the image gradient) takes the upstream scale
+        st.g_rho_adv.mul_(g.to(f))
         # the advection backward also reads the forward's inputs
-        plan.bwd.run(ctx.fwd_key + tuple(t.data_ptr() for t in grads), st.backward)
+        plan.bwd.run(ctx.fwd_key + tuple(t.data_ptr() for t in grads), lambda: st.backward(render=False))
         plan.busy = False
         return grads[0], grads[1], grads[2], grads[3], None, None, None
 

@@ -416,3 +416,37 @@ def test_wait_poll_limit_setting(lib):
     assert lib.ngt_set_wait_polls(default) == default
     from ngt_gb300 import _lib as L
     assert lib.ngt_wait_timeouts(None, 0) == L.NGT_ERR_INVALID_ARGUMENT
+
+
+def test_fused_render_loss_validation(lib):
+    """ngt_raymarch_fwd_l2_bwd rejects null buffers, loss channels out of range and
+    a background without an optical-depth channel before any launch."""
+    from ngt_gb300 import _lib as L
+    g = L.RaymarchGradArgs()
+    a = g.fwd
+    a.dtype = L.F32
+    a.input_shape = L.I64x5(1, 4, 4, 4, 1)
+    a.output_dhw = L.I64x3(4, 4, 4)
+    a.input = ctypes.c_void_p(0x1000)
+    for f in ("matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(a, f, ctypes.c_void_p(0x2000))
+    a.num_cameras = 1
+    a.interpolation, a.boundary, a.blending_mode = 1, 0, 0
+    a.emission_channels = 2
+    a.emission_scale[0], a.emission_scale[1] = 1.0, 1.0
+    g.output, g.output_grad, g.input_grad = ctypes.c_void_p(0x3000), ctypes.c_void_p(0x4000), ctypes.c_void_p(0x5000)
+    tgt, loss = ctypes.c_void_p(0x6000), ctypes.c_void_p(0x7000)
+    assert lib.ngt_raymarch_fwd_l2_bwd(None, None, tgt, 1, loss, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), None, None, 1, loss, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), None, tgt, 3, loss, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"loss_channels" in lib.ngt_last_error_message()
+    # with a background the light channels are 1..Cb-1
+    assert lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), ctypes.c_void_p(0x8000), tgt, 2, loss,
+                                       None) == L.NGT_ERR_INVALID_ARGUMENT
+    a.emission_channels = 0
+    assert lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), ctypes.c_void_p(0x8000), tgt, 1, loss,
+                                       None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"optical depth" in lib.ngt_last_error_message()
+    a.emission_channels = 2
+    g.output_grad = ctypes.c_void_p(0x4002)  # misaligned image gradient
+    assert lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), None, tgt, 1, loss, None) != L.NGT_OK
