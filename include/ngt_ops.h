@@ -498,6 +498,20 @@ int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* scenes, int32_t count, 
  * being built again.  No counterpart in the reference. */
 int ngt_raymarch_bwd_batch_after_fwd(const ngt_raymarch_grad_args* scenes, int32_t count, int32_t blocks_per_sm,
                                      void* workspace, size_t workspace_bytes, void* stream);
+/* The batched render's forward, image L2 loss and backward in one persistent
+ * launch: every (scene, camera, tile) item is marched forward (image written to
+ * the scene's output, loss gradient to its output_grad, 0.5 * the summed squared
+ * difference of the first loss_channels channels to ``targets[i]`` (the scene's
+ * H' x W' x loss_channels per camera) added to *loss) and back by the same
+ * threads, since a pixel's loss gradient depends on that pixel alone; then the
+ * folds.  Scenes as ngt_raymarch_bwd_batch, and one-channel LINEAR density with
+ * emission channels in float or 16-bit storage (the quad layout); workspace of
+ * ngt_raymarch_batch_workspace_bytes.  Replaces ngt_raymarch_fwd_batch +
+ * ngt_image_l2_loss + ngt_raymarch_bwd_batch_after_fwd.  No reference
+ * counterpart (the reference renders one scene per op call). */
+int ngt_raymarch_fwd_l2_bwd_batch(const ngt_raymarch_grad_args* scenes, const void* const* targets, int32_t count,
+                                  int32_t loss_channels, void* loss, int32_t blocks_per_sm, void* workspace,
+                                  size_t workspace_bytes, void* stream);
 
 /* Density warps of many grids: one launch per phase over the concatenated z
  * planes.  The backward takes exact, non-deterministic gradients with all three

@@ -142,6 +142,8 @@ SIGNATURES = {
     "ngt_raymarch_fwd_batch": ([ctypes.POINTER(RaymarchArgs), c_i32, c_i32, c_vp, c_sz, c_vp], c_i32),
     "ngt_raymarch_bwd_batch": ([ctypes.POINTER(RaymarchGradArgs), c_i32, c_i32, c_vp, c_sz, c_vp], c_i32),
     "ngt_raymarch_bwd_batch_after_fwd": ([ctypes.POINTER(RaymarchGradArgs), c_i32, c_i32, c_vp, c_sz, c_vp], c_i32),
+    "ngt_raymarch_fwd_l2_bwd_batch": ([ctypes.POINTER(RaymarchGradArgs), ctypes.POINTER(c_vp), c_i32, c_i32, c_vp,
+                                       c_i32, c_vp, c_sz, c_vp], c_i32),
     "ngt_advect_maccormack_fwd_batch": ([ctypes.POINTER(AdvectArgs), c_i32, c_vp], c_i32),
     "ngt_advect_maccormack_bwd_batch_workspace_bytes": ([ctypes.POINTER(AdvectGradArgs), c_i32], c_sz),
     "ngt_advect_maccormack_bwd_batch": ([ctypes.POINTER(AdvectGradArgs), c_i32, c_vp, c_sz, c_vp], c_i32),

@@ -124,6 +124,10 @@ class BatchedScenes:
             rg.fwd = r
             rg.output, rg.output_grad, rg.input_grad = _ptr(img), _ptr(gimg), _ptr(g_rho_adv)
             rg.grad_mode = L.GRAD["exact"]
+        # every scene's targets within the one target array (the fused render's loss)
+        tsz = self.targets.element_size()
+        starts = [sum(sizes[:k]) for k in range(n)]
+        self.target_ptrs = (ctypes.c_void_p * n)(*[self.targets.data_ptr() + o * tsz for o in starts])
         self.ray_ws = torch.empty(int(self.lib.ngt_raymarch_batch_workspace_bytes(self.ray, n)), dtype=torch.uint8,
                                   device=dev)
         self.adv_ws = torch.empty(int(self.lib.ngt_advect_maccormack_bwd_batch_workspace_bytes(self.adv_g, n)),
@@ -154,7 +158,23 @@ class BatchedScenes:
     def advect_bwd(self, s):
         self._call("ngt_advect_maccormack_bwd_batch", self.adv_g, self.n, _ptr(self.adv_ws), self.adv_ws.numel(), s)
 
+    def render_fused(self, s):
+        """Every scene's render forward, image loss and backward in one persistent
+        launch (each (scene, camera, tile) item marched forward and back by the
+        same threads), then the folds."""
+        self._call("ngt_raymarch_fwd_l2_bwd_batch", self.ray_g, self.target_ptrs, self.n, 1, _ptr(self.loss),
+                   self.blocks_per_sm[1], _ptr(self.ray_ws), self.ray_ws.numel(), s)
+
     def launch(self):
+        s = self._stream()
+        self.loss.zero_()
+        self.advect_fwd(s)
+        self.render_fused(s)
+        self.advect_bwd(s)
+
+    def launch_passes(self):
+        """The same step with the render as three calls: batched forward, one loss
+        call over all images, batched backward reusing the forward's quad layouts."""
         s = self._stream()
         self.loss.zero_()
         self.advect_fwd(s)
@@ -238,12 +258,13 @@ class BatchedScenes:
 
     # -------------------------------------------------------------- autotune
     def autotune(self, candidates=(4, 6, 8, 10, 12, 16), repeats=5):
-        """Time the persistent raymarch passes for each blocks-per-SM setting on
-        these scenes and keep the fastest for the forward and for the backward."""
+        """Time the step's persistent raymarch launch (forward, loss and backward)
+        for each blocks-per-SM setting on these scenes and keep the fastest;
+        returns [(blocks per SM, {setting: ms})]."""
         s = self._stream()
         self.launch()
         best = []
-        for which, fn in ((0, self.render_fwd), (1, self.render_bwd)):
+        for which, fn in ((1, self.render_fused),):
             times = {}
             for c in candidates:
                 self.blocks_per_sm[which] = c

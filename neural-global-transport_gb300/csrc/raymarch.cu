@@ -1119,8 +1119,15 @@ extern "C" int ngt_raymarch_fwd_batch(const ngt_raymarch_args* items, int32_t co
 }
 
 namespace {
+// The fused batch's image L2 loss (ngt_raymarch_fwd_l2_bwd_batch); null for a plain backward.
+struct FusedLossBatch {
+  const void* const* targets;
+  int lc;
+  void* loss;
+};
+
 int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32_t blocks_per_sm, void* workspace,
-                       size_t workspace_bytes, void* stream, bool reuse) {
+                       size_t workspace_bytes, void* stream, bool reuse, const FusedLossBatch* fl = nullptr) {
   if (!items) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null scenes");
   if (count < 1 || count > kMaxBatch) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: 1 to %d scenes", kMaxBatch);
   const ngt_raymarch_args* ptrs[kMaxBatch];
@@ -1135,6 +1142,14 @@ int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32
         g.accumulate)
       return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: exact Beer-Lambert gradients of LINEAR sampling, "
                                        "written");
+    if (fl) {
+      if (!fl->targets[i]) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null target");
+      const int rt = check_aligned("raymarch batch", arith_bytes(g.fwd.dtype), {{"target", fl->targets[i]}});
+      if (rt) return rt;
+      if (!quad_case(&g.fwd))
+        return fail(NGT_ERR_UNSUPPORTED, "raymarch_fwd_l2_bwd_batch: one-channel LINEAR scenes in float or 16-bit "
+                                         "storage (the quad layout); the others take the three batch calls");
+    }
     ptrs[i] = &g.fwd;
   }
   cudaStream_t st = as_stream(stream);
@@ -1144,11 +1159,26 @@ int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32
   if (rc) return rc;
   if (cb < 2) return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: Beer-Lambert needs 2 or 4 blend channels");
   const bool quad = bp.item[0].quad != nullptr;
+  if (fl) {
+    if (cb > 1) {
+      if (fl->lc <= 0 || fl->lc > cb)
+        return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd_batch: loss_channels must be in 1..%d", cb);
+    } else {
+      return fail(NGT_ERR_UNSUPPORTED, "raymarch_fwd_l2_bwd_batch: Beer-Lambert with emission channels");
+    }
+  }
   for (int k = 0; k < count; ++k) {
     RayParams& p = bp.item[k];
     p.out_fwd = items[order[k]].output;
     p.out_grad = items[order[k]].output_grad;
     p.in_grad = items[order[k]].input_grad;
+    if (fl) {  // the forward writes the image and its loss gradient that the backward reads
+      p.output = const_cast<void*>(items[order[k]].output);
+      p.l2_target = fl->targets[order[k]];
+      p.l2_lc = fl->lc;
+      p.l2_grad = const_cast<void*>(items[order[k]].output_grad);
+      p.l2_loss = fl->loss;
+    }
     // the quad path writes every cell gradient in its fold; the direct path adds
     if (!quad && cudaMemsetAsync(p.in_grad, 0, size_t(p.N) * p.din.count() * cin * sizeof(float), st) != cudaSuccess)
       return check_launch("raymarch batch memset");
@@ -1169,12 +1199,24 @@ int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32
   }
   if (rc) return rc;
   const unsigned blocks = persistent_blocks(blocks_per_sm, bp.total);
-  rc = launch_batch_dtype(dtype, BWD_BL, cin, cb, blocks, st, bp);
+  rc = launch_batch_dtype(dtype, fl ? FWD_L2_BWD : BWD_BL, cin, cb, blocks, st, bp);
   if (rc) return rc;
   if (quad) k_quad_fold_batch<<<unsigned(bp.cblock_end[count - 1]), dim3(32, 8), 0, st>>>(bp);
-  return check_launch(reuse ? "ngt_raymarch_bwd_batch_after_fwd" : "ngt_raymarch_bwd_batch");
+  return check_launch(fl ? "ngt_raymarch_fwd_l2_bwd_batch"
+                         : reuse ? "ngt_raymarch_bwd_batch_after_fwd" : "ngt_raymarch_bwd_batch");
 }
 }  // namespace
+
+extern "C" int ngt_raymarch_fwd_l2_bwd_batch(const ngt_raymarch_grad_args* items, const void* const* targets,
+                                             int32_t count, int32_t loss_channels, void* loss, int32_t blocks_per_sm,
+                                             void* workspace, size_t workspace_bytes, void* stream) {
+  if (!targets || !loss) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd_batch: null pointer");
+  if (!items) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null scenes");
+  const int ra = check_aligned("raymarch_fwd_l2_bwd_batch", arith_bytes(items[0].fwd.dtype), {{"loss", loss}});
+  if (ra) return ra;
+  const FusedLossBatch fl = {targets, int(loss_channels), loss};
+  return raymarch_bwd_batch(items, count, blocks_per_sm, workspace, workspace_bytes, stream, false, &fl);
+}
 
 extern "C" int ngt_raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32_t blocks_per_sm,
                                       void* workspace, size_t workspace_bytes, void* stream) {

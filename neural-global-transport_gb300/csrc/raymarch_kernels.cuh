@@ -1034,9 +1034,15 @@ __global__ void __launch_bounds__(kThreads, CIN == 1 ? 8 : 4) k_raymarch_batch(c
     float* dst = reinterpret_cast<float*>(&cam);
     for (int i = threadIdx.x; i < int(sizeof(Cam) / sizeof(float)); i += blockDim.x) dst[i] = __ldg(src + i);
     __syncthreads();
-    if (WHICH == FWD)
+    if (WHICH == FWD) {
       fwd_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
-    else if (checkpointed || CB == 1)
+      continue;
+    }
+    if (WHICH == FWD_L2_BWD) {  // the item's forward and loss, then its backward by the same threads
+      const S l = fwd_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
+      l2_block_add<S>(l, static_cast<S*>(p.l2_loss));
+    }
+    if (checkpointed || CB == 1)
       bwd_exact_tile_call<CIN, CB, T, S>(p, cam, b, oslot, tile);
     else
       bwd_bl_tile<CIN, CB, T, S>(p, cam, b, oslot, tile);
@@ -1063,6 +1069,8 @@ void launch_batch(int which, unsigned blocks, cudaStream_t st, const RayBatch& b
     k_raymarch_batch<CIN, CB, T, S, FWD><<<blocks, kThreads, 0, st>>>(bp);
   } else if (which == BWD_BL) {
     k_raymarch_batch<CIN, CB, T, S, BWD_BL><<<blocks, kThreads, 0, st>>>(bp);
+  } else if (which == FWD_L2_BWD) {
+    k_raymarch_batch<CIN, CB, T, S, FWD_L2_BWD><<<blocks, kThreads, 0, st>>>(bp);
   } else {
     k_extinction_sign_batch<CIN, CB, T><<<dim3(blocks, unsigned(bp.count)), 256, 0, st>>>(bp);
   }

@@ -142,3 +142,27 @@ def test_backward_reuses_forward_quads():
     for k in range(b.n):
         for a, c in zip(got[k], b.gradients(k)):
             assert rel(a, c) < 1e-6
+
+
+@pytest.mark.parametrize("signed", [(), (1,)])
+def test_fused_render_launch_matches_three_calls(signed):
+    """The step's one persistent render launch (forward, loss and backward of every
+    scene, ngt_raymarch_fwd_l2_bwd_batch) equals the batched forward, the loss call
+    and the batched backward; with a scene whose extinction can be negative (its
+    items take the checkpointed adjoint)."""
+    from ngt_gb300.batch import BatchedScenes
+    _, sc = scenes(n=6, seed=21, signed=signed)
+    b = BatchedScenes(sc)
+    b.launch_passes()
+    torch.cuda.synchronize()
+    want = (float(b.loss.item()), b.images.clone(), b.g_images.clone(),
+            [[g.clone() for g in b.gradients(k)] for k in range(b.n)])
+    b.images.fill_(float("nan"))
+    b.g_images.fill_(float("nan"))
+    b.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(b.images, want[1]) and torch.equal(b.g_images, want[2])
+    assert abs(float(b.loss.item()) - want[0]) <= 1e-6 * abs(want[0])
+    for k in range(b.n):
+        for a, c in zip(b.gradients(k), want[3][k]):
+            assert rel(a, c) < 1e-6
