@@ -163,17 +163,18 @@ class ClockSampler:
 # cold cache) on this workload.  They come from a profile, not from the run that
 # prints them; the capture and its date go with the number.
 NCU_TRAFFIC_F32 = {
-    "raymarch_bwd": {"bytes": 90.93e6 + 2.73e6 + 34.10e6,
-                     "kernels": {"k_raymarch_bwd_bl": 93.66e6, "k_quad_fold": 34.10e6},
-                     "kind": "profile", "captured": "2026-12-04",
-                     "profile": "profiles/render_backward_f32_128cube_5views.md"},
+    "raymarch_fwd_l2_bwd": {"bytes": 104.53e6 + 34.16e6 + 34.10e6,
+                            "kernels": {"k_raymarch_fwd_bwd": 138.69e6, "k_quad_fold": 34.10e6},
+                            "kind": "profile", "captured": "2026-12-04",
+                            "profile": "profiles/render_fused_f32_128cube_5views.md"},
 }
-# The resources that bound that call's main kernel (k_raymarch_bwd_bl), from the same
-# capture: L1-to-L2 requests and the L2's atomic unit (its two float4 atomics per sample).
-NCU_LIMITER_F32 = {"raymarch_bwd": {"resource": "L1-to-L2 requests / L2 atomics (float4 quad-gradient atomics)",
-                                    "l1tex2xbar_req_pct": 61.3, "l2_atomic_input_pct": 44.0, "l1tex_pct": 71.1,
-                                    "captured": "2026-12-04",
-                                    "profile": "profiles/render_backward_f32_128cube_5views.md"}}
+# The resources that bound that call's main kernel (k_raymarch_fwd_bwd), from the same
+# capture: L1-to-L2 requests (quad gathers and float4 quad-gradient atomics).
+NCU_LIMITER_F32 = {"raymarch_fwd_l2_bwd": {"resource": "L1-to-L2 requests (quad gathers + float4 atomics)",
+                                           "l1tex2xbar_req_pct": 58.2, "lsu_wavefronts_pct": 48.6,
+                                           "l2_atomic_input_pct": 32.6, "l1tex_pct": 65.3,
+                                           "captured": "2026-12-04",
+                                           "profile": "profiles/render_fused_f32_128cube_5views.md"}}
 
 
 def measured_peak_hbm():
