@@ -239,9 +239,11 @@ typedef struct {
    * 16x8-pixel tiles x 128 rays x D' floats) room for every ray's first D'
    * density samples.  A Beer-Lambert forward with emission through that buffer
    * stores them (a warp's 32 rays interleaved: 128 contiguous bytes per step)
-   * and tags the buffer with its ray table; the one-pass exact backward of the
-   * same quad buffer and ray table reads them instead of gathering each
-   * sample's corners again.  ngt_raymarch_quad clears the tag.  The samples
+   * and tags the buffer with its ray table's address and its sizes; the
+   * one-pass exact backward of the same quad buffer, ray table and sizes reads
+   * them instead of gathering each sample's corners again.  ngt_raymarch_quad
+   * clears the tag; the buffer must be sized (ngt_raymarch_quad_bytes) with the
+   * args of the calls that use it, as for the quad layout itself.  The samples
    * are the forward's own values, so the gradient is unchanged.  0: the
    * backward gathers. */
   int32_t sample_cache;

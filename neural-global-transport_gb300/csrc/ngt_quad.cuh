@@ -102,7 +102,7 @@ __device__ __forceinline__ void quad_build_at(const T* __restrict__ g, const Dim
 
 // Planes of entries one thread of k_quad_build fills (the (x, y) boundary
 // mapping and the sign vote are then shared by those planes).
-constexpr int kQuadPlanes = 4;
+constexpr int kQuadPlanes = 8;
 
 // One thread per (xq, yq) and kQuadPlanes consecutive planes of the N * (D + 2)
 // planes (blockIdx.z = first plane / kQuadPlanes); quad_build_at's entries.

@@ -422,17 +422,29 @@ size_t samples_bytes(const ngt_raymarch_args* a) {
   return align256(size_t(slots_of(a) * tiles * kThreads * a->output_dhw[0]) * sizeof(float));
 }
 
+// SplitMix64's finaliser (a published 64-bit mixing function).
+uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
 // Points p at the sample cache of the prepared layout ``a->quad`` when this
 // call can keep or use it: one-channel Beer-Lambert with emission through a
-// prepared layout sized with sample_cache, and a ray table (whose address tags
-// the cache: a forward of other rays overwrites the tag).
+// prepared layout sized with sample_cache, and a ray table.  The tag mixes the
+// table's address with the render's depth, image and slot counts (the cache's
+// layout), so a forward of other rays overwrites it and a call of other sizes
+// does not match it; it is odd, never the cleared 0.
 void use_sample_cache(const ngt_raymarch_args* a, int cb, RayParams& p) {
   if (!a->quad || !a->sample_cache || !a->rays || !quad_case(a) || a->blending_mode != NGT_BEER_LAMBERT || cb < 2)
     return;
   char* q = const_cast<char*>(static_cast<const char*>(a->quad));
   p.samples = reinterpret_cast<float*>(q + kQuadHeader + quad_bytes(a));
   p.sample_word = reinterpret_cast<unsigned long long*>(q + kSampleTagOffset);
-  p.sample_tag = static_cast<unsigned long long>(reinterpret_cast<uintptr_t>(a->rays)) | 1ull;
+  uint64_t t = mix64(uint64_t(reinterpret_cast<uintptr_t>(a->rays)));
+  for (const int64_t v : {a->output_dhw[0], a->output_dhw[1], a->output_dhw[2], slots_of(a)})
+    t = mix64(t ^ uint64_t(v));
+  p.sample_tag = static_cast<unsigned long long>(t | 1ull);
 }
 
 int check_prepared_quad(const ngt_raymarch_args* a) {

@@ -99,9 +99,9 @@ def test_cached_samples_give_the_same_image_and_gradient(dtype, bm):
     gy = torch.as_tensor(RNG.standard_normal(tuple(y0.shape)).astype(np.float32), device="cuda")
     g0, g1 = plain.backward(y0, gy), cached.backward(y1, gy)
     assert rel(g1, g0) < 1e-6
-    # the tag word the forward wrote: the ray table's address (odd)
+    # the forward tagged the cache (an odd word: its ray table and sizes mixed)
     tag = int(cached.quad[8:16].view(torch.int64).item())
-    assert tag == cached.r.rays | 1
+    assert tag & 1
 
 
 def test_cache_of_another_density_is_not_used():
@@ -132,7 +132,8 @@ def test_cache_of_other_rays_is_not_used():
     y = first.forward()
     gy = torch.as_tensor(RNG.standard_normal(tuple(y.shape)).astype(np.float32), device="cuda")
     want = first.backward(y, gy)  # from the cache
+    tag_first = int(first.quad[8:16].view(torch.int64).item())
     other.forward()
-    assert int(first.quad[8:16].view(torch.int64).item()) == other.r.rays | 1
+    assert int(first.quad[8:16].view(torch.int64).item()) not in (0, tag_first)
     got = first.backward(y, gy)  # the tag names the other rays: gathers
     assert rel(got, want) < 1e-6
