@@ -755,7 +755,8 @@ bool fused_launch(const ngt_raymarch_grad_args* a) {
   return a->grad_mode == NGT_GRAD_EXACT && !a->deterministic && quad_case(&a->fwd) && needs_sign_flag(a);
 }
 
-int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void* stream);
+// ``check_only``: validate the arguments and return before any launch.
+int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void* stream, bool check_only = false);
 }  // namespace
 
 extern "C" int ngt_raymarch_bwd(const ngt_raymarch_grad_args* a, void* stream) {
@@ -786,7 +787,9 @@ extern "C" int ngt_raymarch_fwd_l2_bwd(const ngt_raymarch_grad_args* a, const vo
     return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd: loss_channels must be in 1..%d", top);
   const FusedLoss fl = {target, int(loss_channels), loss, background};
   if (!fused_launch(a)) {
-    // the two passes: the forward with its loss, then the backward
+    // the two passes: the forward with its loss, then the backward (whose arguments
+    // are checked first, so that a rejected call launches nothing)
+    if ((rc = raymarch_bwd_impl(a, nullptr, stream, true))) return rc;
     ngt_raymarch_args f = a->fwd;
     f.output = const_cast<void*>(a->output);
     void* ig = const_cast<void*>(a->output_grad);
@@ -799,7 +802,7 @@ extern "C" int ngt_raymarch_fwd_l2_bwd(const ngt_raymarch_grad_args* a, const vo
 }
 
 namespace {
-int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void* stream) {
+int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void* stream, bool check_only) {
   int cin, cb;
   int rc = validate(&a->fwd, cin, cb);
   if (rc) return rc;
@@ -820,6 +823,7 @@ int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void
   const Layout l = bwd_layout(a);
   if (!a->workspace || a->workspace_bytes < l.total)
     return fail(NGT_ERR_WORKSPACE, "raymarch_bwd: needs %zu workspace bytes", l.total);
+  if (check_only) return NGT_OK;
   RayParams p = make_params(&a->fwd);
   p.order = ray_order(&a->fwd);
   p.out_fwd = a->output;

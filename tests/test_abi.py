@@ -450,3 +450,26 @@ def test_fused_render_loss_validation(lib):
     a.emission_channels = 2
     g.output_grad = ctypes.c_void_p(0x4002)  # misaligned image gradient
     assert lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), None, tgt, 1, loss, None) != L.NGT_OK
+
+
+def test_fused_render_fallback_checks_backward_first(lib):
+    """A call that runs as two passes (reference gradient here) rejects a short
+    backward workspace before its forward launches anything."""
+    from ngt_gb300 import _lib as L
+    g = L.RaymarchGradArgs()
+    a = g.fwd
+    a.dtype = L.F32
+    a.input_shape = L.I64x5(1, 4, 4, 4, 1)
+    a.output_dhw = L.I64x3(4, 4, 4)
+    a.input = ctypes.c_void_p(0x1000)
+    for f in ("matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(a, f, ctypes.c_void_p(0x2000))
+    a.num_cameras = 1
+    a.interpolation, a.boundary, a.blending_mode = 1, 0, 0
+    a.emission_channels = 2
+    a.emission_scale[0], a.emission_scale[1] = 1.0, 1.0
+    g.output, g.output_grad, g.input_grad = ctypes.c_void_p(0x3000), ctypes.c_void_p(0x4000), ctypes.c_void_p(0x5000)
+    g.grad_mode = L.GRAD["reference"]
+    g.workspace, g.workspace_bytes = ctypes.c_void_p(0x6000), 16
+    rc = lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), None, ctypes.c_void_p(0x7000), 1, ctypes.c_void_p(0x8000), None)
+    assert rc == L.NGT_ERR_WORKSPACE
