@@ -67,7 +67,8 @@ def parse():
     ap.add_argument("--impl", default="ngt", choices=["ngt", "reference"])
     ap.add_argument("--grad-mode", default="exact", choices=["exact", "reference"])
     ap.add_argument("--no-graph", action="store_true")
-    ap.add_argument("--cpu-baseline", default="on", choices=["on", "off"])
+    # "full": also the same step in one process (about a minute of host time), beside the split over every core
+    ap.add_argument("--cpu-baseline", default="on", choices=["on", "off", "full"])
     ap.add_argument("--kernel-stats", default="on", choices=["on", "off"])
     ap.add_argument("--workload", default="step", choices=["step", "chain", "large", "batch", "velocity"],
                     help="step: the headline differentiated step; chain: the checkpointed 120-frame plume "
@@ -361,17 +362,27 @@ def gpu_arm(args, world, rank, local):
     line["e2e_ops"] = e2e_ops
     if e2e_step:
         line["e2e_step"] = e2e_step
-    if rank == 0 and world == 1 and args.cpu_baseline == "on":
+    if rank == 0 and world == 1 and args.cpu_baseline in ("on", "full"):
         from oracle import parallel
+        targets = np.ascontiguousarray(tgt.cpu().numpy())
         pool, nproc = parallel.make_pool()  # spawned workers: no CUDA in them
         try:
-            t = cpu_step(pool, nproc, w, np.ascontiguousarray(tgt.cpu().numpy()))
+            t = cpu_step(pool, nproc, w, targets)
         finally:
             pool.close()
             pool.join()
         line["cpu_baseline"] = {"value": 1.0 / t, "unit": "steps/s", "cores": nproc, "kind": "port",
                                 "sample": CPU_SAMPLE % nproc + "; the same inputs and targets as the GPU step",
                                 "host": host_cpu()}
+        if args.cpu_baseline == "full":
+            pool1, _ = parallel.make_pool(1)
+            try:
+                t1 = cpu_step(pool1, 1, w, targets)
+            finally:
+                pool1.close()
+                pool1.join()
+            line["cpu_baseline"]["single_process"] = {"value": 1.0 / t1, "unit": "steps/s", "seconds": t1,
+                                                      "sample": "the same full step in one process"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
