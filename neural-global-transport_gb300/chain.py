@@ -27,7 +27,7 @@ import ctypes
 import torch
 
 from . import _lib as L
-from .ops import _code, _ptr
+from .ops import _code, _ptr, sample_cache_pays
 
 
 class AdvectRenderChain:
@@ -126,7 +126,8 @@ class AdvectRenderChain:
             r.blending_mode, r.keep_dims, r.separate_camera_batch = L.BLEND["BEER_LAMBERT"], 0, 1
             r.emission_channels = 2
             r.emission_scale[0], r.emission_scale[1] = light * depth_step, depth_step
-            r.sample_cache = 1  # the render backward reads its forward's samples
+            # the render backward reads its forward's samples back where that pays
+            r.sample_cache = int(sample_cache_pays((D, H, W), 1, rho0.dtype, dev))
             return r
 
         self.ray = [ray_args(self.seg[j + 1]) for j in range(K)]

@@ -179,6 +179,23 @@ def _cameras(r, M, V, P, F):
     return cams
 
 
+def sample_cache_pays(grid_dhw, batch, dtype, device):
+    """Whether the render's sample cache (``ngt_raymarch_args.sample_cache``) is
+    worth its L2 footprint: always for float storage, and for 16-bit storage while
+    the quad gradient (16 bytes per (x, y)-quad and plane) fits in the L2 -- beyond
+    that, 16-bit storage's 8-byte quad gathers cost less than the cache (measured
+    both ways at 128^3 and at 256x448x256)."""
+    if dtype == torch.float32:
+        return True
+    D, H, W = (int(v) for v in grid_dhw)
+    gquad = int(batch) * (W + 1) * (H + 1) * (D + 2) * 16
+    try:
+        l2 = int(getattr(torch.cuda.get_device_properties(device), "L2_cache_size", 0)) or (128 << 20)
+    except (RuntimeError, AssertionError):
+        l2 = 128 << 20
+    return gquad <= l2
+
+
 def _rays(r, M, V, P, F):
     """The ray table of raymarch args ``r`` (ngt_raymarch_rays: every ray set up in
     double precision) when all four matrix buffers are cached host uploads,
@@ -488,7 +505,8 @@ def _ray_forward(input, M, V, P, F, out_dhw, a, keep_quad=False):
     lib = L.load()
     quad = None
     if keep_quad:
-        r.sample_cache = int(rays is not None)
+        r.sample_cache = int(rays is not None and sample_cache_pays(input.shape[1:4], input.shape[0], input.dtype,
+                                                                     input.device))
         nq = int(lib.ngt_raymarch_quad_bytes(ctypes.byref(r)))
         if nq:
             buf = torch.empty(nq, dtype=torch.uint8, device=input.device)

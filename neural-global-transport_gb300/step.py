@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
-from .ops import _code, _ptr
+from .ops import _code, _ptr, sample_cache_pays
 
 
 class RenderAdvectStep:
@@ -114,8 +114,8 @@ class RenderAdvectStep:
         # the advected density in the quad gather layout, prepared once per step for
         # the render's forward and backward; with the exact backward it also keeps
         # the forward's density samples, which the one-pass adjoint reads back
-        # instead of gathering them again
-        r.sample_cache = 1 if grad_mode == "exact" else 0
+        # instead of gathering them again, where that pays (ops.sample_cache_pays)
+        r.sample_cache = int(grad_mode == "exact" and sample_cache_pays((D, H, W), 1, rho.dtype, dev))
         nq = int(self.lib.ngt_raymarch_quad_bytes(ctypes.byref(r)))
         self.ray_quad = torch.empty(nq, dtype=torch.uint8, device=dev) if nq else None
         if nq:

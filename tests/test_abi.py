@@ -473,3 +473,16 @@ def test_fused_render_fallback_checks_backward_first(lib):
     g.workspace, g.workspace_bytes = ctypes.c_void_p(0x6000), 16
     rc = lib.ngt_raymarch_fwd_l2_bwd(ctypes.byref(g), None, ctypes.c_void_p(0x7000), 1, ctypes.c_void_p(0x8000), None)
     assert rc == L.NGT_ERR_WORKSPACE
+
+
+def test_sample_cache_policy():
+    """The render keeps its sample cache for float storage, and for 16-bit storage
+    while the quad gradient fits in the L2 (host logic; without a GPU the L2 is
+    taken as 128 MiB)."""
+    import torch
+    from ngt_gb300.ops import sample_cache_pays
+    dev = torch.device("cuda", 0) if torch.cuda.is_available() else torch.device("cpu")
+    assert sample_cache_pays((256, 448, 256), 1, torch.float32, dev)
+    assert sample_cache_pays((128, 128, 128), 1, torch.bfloat16, dev)    # 34 MB quad gradient
+    assert not sample_cache_pays((256, 448, 256), 1, torch.float16, dev)  # 476 MB
+    assert not sample_cache_pays((128, 128, 128), 8, torch.bfloat16, dev)  # 8 grids: 272 MB
