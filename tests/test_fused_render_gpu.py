@@ -17,7 +17,7 @@ CAM = (14, 18, 22)  # depth samples, image height, width
 YAWS = (10, -50, 95)
 
 
-def setup(dtype, cache, seed=0):
+def setup(dtype, cache, seed=0, prepared=True):
     from ngt_gb300 import _lib as L
     from ngt_gb300 import ops, scene
     rng = np.random.default_rng(seed)
@@ -36,9 +36,16 @@ def setup(dtype, cache, seed=0):
     assert lib.ngt_raymarch_rays(ctypes.byref(r), ops._ptr(rays), st) == L.NGT_OK
     r.rays = ops._ptr(rays)
     r.sample_cache = int(cache)
-    quad = torch.empty(int(lib.ngt_raymarch_quad_bytes(ctypes.byref(r))), dtype=torch.uint8, device="cuda")
-    assert lib.ngt_raymarch_quad(ctypes.byref(r), ops._ptr(quad), st) == L.NGT_OK
-    r.quad = ops._ptr(quad)
+    quad = None
+    if prepared:
+        quad = torch.empty(int(lib.ngt_raymarch_quad_bytes(ctypes.byref(r))), dtype=torch.uint8, device="cuda")
+        assert lib.ngt_raymarch_quad(ctypes.byref(r), ops._ptr(quad), st) == L.NGT_OK
+        r.quad = ops._ptr(quad)
+    else:
+        # the separate forward builds its quad layout in its workspace, as the fused call does in its own
+        quad = torch.empty(int(lib.ngt_raymarch_fwd_workspace_bytes(ctypes.byref(r))), dtype=torch.uint8,
+                           device="cuda")
+        r.workspace, r.workspace_bytes = ops._ptr(quad), quad.numel()
     target = torch.as_tensor(rng.uniform(0, 0.5, (1, len(YAWS)) + CAM[1:] + (1,)).astype(np.float32), device="cuda")
     bkg = torch.as_tensor(rng.uniform(0, 0.4, (len(YAWS),) + CAM[1:] + (1,)).astype(np.float32), device="cuda")
     return dict(L=L, ops=ops, lib=lib, st=st, x=x, r=r, keep=(rays, quad, mats), target=target, bkg=bkg)
@@ -114,3 +121,14 @@ def test_unfused_settings_run_the_two_passes(mode, det):
         assert torch.equal(g0, g1)  # the deterministic gradient: the same bits
     else:
         assert rel(g1, g0) < 1e-6
+
+
+def test_fused_without_prepared_quad():
+    """Without a prepared quad layout the fused call builds its own in the workspace
+    (no sample cache) and still equals the separate calls."""
+    c = setup(torch.float32, 0, seed=6, prepared=False)
+    y0, gy0, l0, g0 = separate(c, False)
+    y1, gy1, l1, g1 = fused(c, False)
+    assert torch.equal(y0, y1) and torch.equal(gy0, gy1)
+    assert abs(float(l1) - float(l0)) <= 1e-6 * abs(float(l0))
+    assert rel(g1, g0) < 1e-6
