@@ -17,7 +17,7 @@ CAM = (14, 18, 22)  # depth samples, image height, width
 YAWS = (10, -50, 95)
 
 
-def setup(dtype, cache, seed=0, prepared=True):
+def setup(dtype, cache, seed=0, prepared=True, bm="BORDER"):
     from ngt_gb300 import _lib as L
     from ngt_gb300 import ops, scene
     rng = np.random.default_rng(seed)
@@ -27,7 +27,7 @@ def setup(dtype, cache, seed=0, prepared=True):
     M = scene.model_params([vol])
     V, P, F = scene.camera_params(cams)
     mats = [ops._floats(m, w, x.device) for m, w in ((M, 16), (V, 16), (P, 16), (F, 6))]
-    attrs = dict(interpolation="LINEAR", boundary="BORDER", blending_mode="BEER_LAMBERT", keep_dims=False,
+    attrs = dict(interpolation="LINEAR", boundary=bm, blending_mode="BEER_LAMBERT", keep_dims=False,
                  separate_camera_batch=True, emission_scale=(0.6, 1.2))
     y = torch.empty((1, len(YAWS)) + CAM[1:] + (2,), device="cuda")
     r = ops._ray_args(x, *mats, list(CAM), y, attrs)
@@ -127,6 +127,18 @@ def test_fused_without_prepared_quad():
     """Without a prepared quad layout the fused call builds its own in the workspace
     (no sample cache) and still equals the separate calls."""
     c = setup(torch.float32, 0, seed=6, prepared=False)
+    y0, gy0, l0, g0 = separate(c, False)
+    y1, gy1, l1, g1 = fused(c, False)
+    assert torch.equal(y0, y1) and torch.equal(gy0, gy1)
+    assert abs(float(l1) - float(l0)) <= 1e-6 * abs(float(l0))
+    assert rel(g1, g0) < 1e-6
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "WRAP"])
+def test_fused_other_boundaries(bm):
+    """CLAMP and WRAP rays (never clipped: every ray takes the frustum's depth
+    samples, the quad layout's padding maps the outside cells)."""
+    c = setup(torch.float32, 1, seed=8, bm=bm)
     y0, gy0, l0, g0 = separate(c, False)
     y1, gy1, l1, g1 = fused(c, False)
     assert torch.equal(y0, y1) and torch.equal(gy0, gy1)
