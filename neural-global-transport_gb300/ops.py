@@ -15,6 +15,7 @@ All tensors must be contiguous CUDA tensors; there is no CPU path.
 import collections
 import contextlib
 import ctypes
+import functools
 
 import numpy as np
 import torch
@@ -189,11 +190,17 @@ def sample_cache_pays(grid_dhw, batch, dtype, device):
         return True
     D, H, W = (int(v) for v in grid_dhw)
     gquad = int(batch) * (W + 1) * (H + 1) * (D + 2) * 16
+    return gquad <= _l2_bytes(torch.device(device).index if torch.device(device).type == "cuda" else -1)
+
+
+@functools.lru_cache(maxsize=None)
+def _l2_bytes(index):
+    """L2 size of CUDA device ``index`` (128 MiB when it cannot be read)."""
     try:
-        l2 = int(getattr(torch.cuda.get_device_properties(device), "L2_cache_size", 0)) or (128 << 20)
+        dev = torch.device("cuda", index if index is not None and index >= 0 else torch.cuda.current_device())
+        return int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0)) or (128 << 20)
     except (RuntimeError, AssertionError):
-        l2 = 128 << 20
-    return gquad <= l2
+        return 128 << 20
 
 
 def _rays(r, M, V, P, F):
