@@ -691,6 +691,72 @@ __global__ void __launch_bounds__(kBlock) k_face_lut_adjoint(const S* __restrict
   }
 }
 
+// The exact lookup adjoint of all three components in gather form, for the
+// faces of component s: the scatter of k_face_lut_adjoint reversed.  Component
+// tgt's lookup resamples s at p = X + o with o = +1/2 along s, -1/2 along tgt and
+// 0 along the third axis c (comp_offset): corners X_s, X_s + 1 and X_t - 1, X_t
+// with weight 1/2 each, X_c with weight 1 (tri_setup; the ceil corner of the
+// integer axis has weight 0).  Face F of s therefore gathers 1/4 of
+// glut_tgt[X][s] from X_c = F_c, X_s in {F_s - 1, F_s} and the X_t whose t
+// corners the boundary rule maps onto F_t -- X_t = F_t (its upper corner),
+// X_t = F_t + 1 (its lower corner) and, at the edges, the clamped or wrapped
+// corners; under BORDER the sample X_t = dims_t (outside: p + 1/2 = dims_t) and
+// the lower corner of X_t = 0 drop out.  Plus the component's own lookup
+// entry.  No atomics: one thread per face adds -dt times its sum to gu_s.
+template <class S, int s>
+__global__ void __launch_bounds__(kBlock) k_face_lut_gather(const S* __restrict__ glut0, const S* __restrict__ glut1,
+                                                            const S* __restrict__ glut2, S* __restrict__ gus,
+                                                            Dims cells, int bm, float dt) {
+  const Dims d = face_dims(cells, s);
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= d.count()) return;
+  int F[3];
+  cell_of(i, d, F[0], F[1], F[2]);
+  const S* glut[3] = {glut0, glut1, glut2};
+  const int n[3] = {d.x, d.y, d.z};
+  S acc = S(0);
+#pragma unroll
+  for (int tgt = 0; tgt < 3; ++tgt) {
+    if (tgt == s) continue;
+    const int c = 3 - s - tgt;
+    const Dims T = face_dims(cells, tgt);
+    const int nt = n[tgt];  // faces of s along tgt (tgt's lattice has nt + 1)
+    // the X_t whose t corners land on F_t (at most four; both edge rules apply
+    // to the one face of a single cell)
+    int xt[4];
+    int m = 0;
+    const int ft = F[tgt];
+    xt[m++] = ft;  // upper corner X_t = F_t (inside under BORDER: ft <= nt - 1)
+    if (bm != BORDER || ft + 1 <= nt - 1) xt[m++] = ft + 1;  // lower corner X_t - 1 = F_t
+    if (bm == CLAMP) {
+      if (ft == 0) xt[m++] = 0;        // lower corner -1 clamps to 0
+      if (ft == nt - 1) xt[m++] = nt;  // upper corner nt clamps to nt - 1
+    } else if (bm == WRAP) {
+      if (ft == nt - 1) xt[m++] = 0;  // lower corner -1 wraps to nt - 1
+      if (ft == 0) xt[m++] = nt;      // upper corner nt wraps to 0
+    }
+    S part = S(0);
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+      const int xs = F[s] - 1 + ks;
+      const int ns = s == 0 ? T.x : s == 1 ? T.y : T.z;
+      if (xs < 0 || xs >= ns) continue;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k >= m) break;
+        int X[3];
+        X[s] = xs;
+        X[tgt] = xt[k];
+        X[c] = F[c];
+        part += glut[tgt][flat(X[0], X[1], X[2], T) * 3 + s];
+      }
+    }
+    acc += S(0.25) * part;
+  }
+  acc += glut[s][i * 3 + s];
+  gus[i] += -(acc * S(dt));
+}
+
 // ---------------------------------------------------- batched density warps
 // Many grids of different sizes in one launch per phase: blockIdx.z runs over
 // the concatenated z planes of all grids, blockIdx.x / y over the largest grid's
@@ -1066,8 +1132,13 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
   char* w = static_cast<char*>(g->workspace);
   S* gfwd = reinterpret_cast<S*>(w);
   w += size_t(nmax) * sizeof(S);
-  S* glut = reinterpret_cast<S*>(w);
-  w += size_t(nmax) * 3 * sizeof(S);
+  // the exact gradient keeps every component's lookup gradient for the gather
+  S* gluts[3];
+  for (int c = 0; c < 3; ++c) {
+    gluts[c] = reinterpret_cast<S*>(w);
+    if (!reference || c == 2) w += size_t(nmax) * 3 * sizeof(S);
+  }
+  S* glut = gluts[0];
   S* buf = nullptr;
   unsigned* cnt = nullptr;
   if (reference) {
@@ -1085,7 +1156,7 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
     p.gout = static_cast<const S*>(go[c]);
     p.gdata = gu[c];
     p.gfwd = gfwd;
-    p.glut = glut;
+    p.glut = reference ? glut : gluts[c];
     p.reference = reference;
     p.buf = buf;
     p.cnt = cnt;
@@ -1094,8 +1165,9 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
                  ? launch_bwd12<1, T>(p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup[c]), p.d}, st)
                  : launch_bwd12<1, T>(p, face_lookup<T>(a, c), st);
     if (rc) return rc;
-    if (reference && (cudaMemsetAsync(buf, 0, size_t(nall) * sizeof(S), st) != cudaSuccess ||
-                      cudaMemsetAsync(cnt, 0, size_t(nall) * sizeof(unsigned), st) != cudaSuccess))
+    if (!reference) continue;  // the exact lookup adjoint gathers once every component's is there
+    if (cudaMemsetAsync(buf, 0, size_t(nall) * sizeof(S), st) != cudaSuccess ||
+        cudaMemsetAsync(cnt, 0, size_t(nall) * sizeof(unsigned), st) != cudaSuccess)
       return check_launch("advect_velocity_bwd memset");
     k_face_lut_adjoint<S><<<ceil_div_u(p.d.count(), kBlock), kBlock, 0, st>>>(glut, gu[0], gu[1], gu[2], cells, c,
                                                                                a->boundary, a->dt, reference, buf, cnt);
@@ -1107,6 +1179,14 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
         off += ns;
       }
     }
+  }
+  if (!reference) {
+    const unsigned b0 = ceil_div_u(face_dims(cells, 0).count(), kBlock);
+    const unsigned b1 = ceil_div_u(face_dims(cells, 1).count(), kBlock);
+    const unsigned b2 = ceil_div_u(face_dims(cells, 2).count(), kBlock);
+    k_face_lut_gather<S, 0><<<b0, kBlock, 0, st>>>(gluts[0], gluts[1], gluts[2], gu[0], cells, a->boundary, a->dt);
+    k_face_lut_gather<S, 1><<<b1, kBlock, 0, st>>>(gluts[0], gluts[1], gluts[2], gu[1], cells, a->boundary, a->dt);
+    k_face_lut_gather<S, 2><<<b2, kBlock, 0, st>>>(gluts[0], gluts[1], gluts[2], gu[2], cells, a->boundary, a->dt);
   }
   return check_launch("ngt_advect_velocity_bwd");
 }
@@ -1318,8 +1398,10 @@ extern "C" int ngt_advect_velocity_fwd(const ngt_advect_velocity_args* a, void* 
 extern "C" size_t ngt_advect_velocity_bwd_workspace_bytes(const ngt_advect_velocity_grad_args* g) {
   if (!g) return 0;
   const size_t cs = compute_size(g->fwd.dtype);
-  size_t bytes = size_t(max_faces(g->fwd.grid_dhw)) * 4 * cs;
-  if (g->grad_mode == NGT_GRAD_REFERENCE) bytes += size_t(all_faces(g->fwd.grid_dhw)) * (cs + sizeof(unsigned));
+  // fwd-field gradient, lookup gradients (every component's for the exact gather, one for the reference scatter)
+  const bool reference = g->grad_mode == NGT_GRAD_REFERENCE;
+  size_t bytes = size_t(max_faces(g->fwd.grid_dhw)) * (reference ? 4 : 10) * cs;
+  if (reference) bytes += size_t(all_faces(g->fwd.grid_dhw)) * (cs + sizeof(unsigned));
   return bytes;
 }
 

@@ -616,7 +616,7 @@ def test_velocity_advect_forward_bitexact(bm, order, clamp):
         assert np.array_equal(N(o), r)
 
 
-@pytest.mark.parametrize("bm", ["CLAMP", "BORDER"])
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
 @pytest.mark.parametrize("mode", ["exact", "reference"])
 def test_velocity_advect_backward(bm, mode):
     from ngt_gb300 import advect, ops
@@ -627,6 +627,22 @@ def test_velocity_advect_backward(bm, mode):
         out = advect.warp_velocity(*ts, boundary=bm)
         torch.autograd.backward(out, [T(g) for g in gs])
     ref = oadvect.velocity_maccormack_grad(ux, uy, uz, gs, boundary=bm, grad_mode=mode)
+    for t, r in zip(ts, ref):
+        assert rel(r, N(t.grad)) < 1e-4
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
+@pytest.mark.parametrize("shape", [(1, 6, 7), (5, 1, 6), (4, 6, 1)])
+def test_velocity_advect_backward_single_cell_axis(bm, shape):
+    """Grids one cell thick along an axis: the lookup adjoint's clamped and wrapped
+    corners of both edges land on the same faces."""
+    from ngt_gb300 import advect
+    _, ux, uy, uz = advect_inputs(shape=shape, seed=23, max_u=1.0)
+    gs = [RNG.standard_normal(u.shape).astype(np.float32) for u in (ux, uy, uz)]
+    ts = [T(u).requires_grad_() for u in (ux, uy, uz)]
+    out = advect.warp_velocity(*ts, boundary=bm)
+    torch.autograd.backward(out, [T(g) for g in gs])
+    ref = oadvect.velocity_maccormack_grad(ux, uy, uz, gs, boundary=bm, grad_mode="exact")
     for t, r in zip(ts, ref):
         assert rel(r, N(t.grad)) < 1e-4
 
