@@ -439,9 +439,17 @@ def e2e_measure(torch, dev, w, st, tgt, args, flush, fused=True):
     host = [torch.as_tensor(a).to(st).pin_memory() for a in (w.rho, w.ux, w.uy, w.uz)]
     h2d = sum(t.numel() * t.element_size() for t in host)
     scale = (w.depth_step, w.depth_step)
+    # the optimisation's density and velocity: device tensors that require grad,
+    # as an optimiser keeps them; every step copies its inputs into them from
+    # pinned host memory and clears their gradients
+    ts = [torch.empty(t.shape, dtype=t.dtype, device=dev).requires_grad_() for t in host]
 
     def one():
-        ts = [t.to(dev, non_blocking=True).requires_grad_() for t in host]
+        with torch.no_grad():
+            for d, h in zip(ts, host):
+                d.copy_(h, non_blocking=True)
+        for d in ts:
+            d.grad = None
         if fused:
             loss = render_advect_loss(ts[0], ts[1], ts[2], ts[3], w.M, w.V, w.P, w.F, tgt, w.image_dhw)
         else:
@@ -464,6 +472,7 @@ def e2e_measure(torch, dev, w, st, tgt, args, flush, fused=True):
         tot += time.perf_counter() - t0
     path = ("ngt_gb300.step.render_advect_loss (one autograd node), loss.backward()" if fused else
             "ngt_gb300.advect.warp + ngt_gb300.ops.raymarch_grid_transform + ops.image_l2_loss, loss.backward()")
+    path += "; inputs copied into the optimisation's device tensors every step"
     return {"value": n / tot, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4, "path": path}
 
 
