@@ -1159,6 +1159,12 @@ int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32
       return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: exact Beer-Lambert gradients of LINEAR sampling, "
                                        "written");
     if (fl) {
+      // (checked before make_batch launches anything)
+      const int cbi = g.fwd.emission_channels ? g.fwd.emission_channels : int(g.fwd.input_shape[4]);
+      if (cbi < 2)
+        return fail(NGT_ERR_UNSUPPORTED, "raymarch_fwd_l2_bwd_batch: Beer-Lambert with emission channels");
+      if (fl->lc <= 0 || fl->lc > cbi)
+        return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd_batch: loss_channels must be in 1..%d", cbi);
       if (!fl->targets[i]) return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch batch: null target");
       const int rt = check_aligned("raymarch batch", arith_bytes(g.fwd.dtype), {{"target", fl->targets[i]}});
       if (rt) return rt;
@@ -1175,14 +1181,6 @@ int raymarch_bwd_batch(const ngt_raymarch_grad_args* items, int32_t count, int32
   if (rc) return rc;
   if (cb < 2) return fail(NGT_ERR_UNSUPPORTED, "raymarch batch backward: Beer-Lambert needs 2 or 4 blend channels");
   const bool quad = bp.item[0].quad != nullptr;
-  if (fl) {
-    if (cb > 1) {
-      if (fl->lc <= 0 || fl->lc > cb)
-        return fail(NGT_ERR_INVALID_ARGUMENT, "raymarch_fwd_l2_bwd_batch: loss_channels must be in 1..%d", cb);
-    } else {
-      return fail(NGT_ERR_UNSUPPORTED, "raymarch_fwd_l2_bwd_batch: Beer-Lambert with emission channels");
-    }
-  }
   for (int k = 0; k < count; ++k) {
     RayParams& p = bp.item[k];
     p.out_fwd = items[order[k]].output;

@@ -486,3 +486,32 @@ def test_sample_cache_policy():
     assert sample_cache_pays((128, 128, 128), 1, torch.bfloat16, dev)    # 34 MB quad gradient
     assert not sample_cache_pays((256, 448, 256), 1, torch.float16, dev)  # 476 MB
     assert not sample_cache_pays((128, 128, 128), 8, torch.bfloat16, dev)  # 8 grids: 272 MB
+
+
+def test_fused_batch_validation(lib):
+    """ngt_raymarch_fwd_l2_bwd_batch rejects loss channels out of range, scenes
+    without emission channels and null targets before any launch."""
+    from ngt_gb300 import _lib as L
+    g = (L.RaymarchGradArgs * 1)()
+    a = g[0].fwd
+    a.dtype = L.F32
+    a.input_shape = L.I64x5(1, 4, 4, 4, 1)
+    a.output_dhw = L.I64x3(4, 4, 4)
+    a.input = ctypes.c_void_p(0x1000)
+    for f in ("matrix_m", "matrix_v", "matrix_p", "frustum"):
+        setattr(a, f, ctypes.c_void_p(0x2000))
+    a.num_cameras = 1
+    a.interpolation, a.boundary, a.blending_mode = 1, 0, 0
+    a.emission_channels = 2
+    a.emission_scale[0], a.emission_scale[1] = 1.0, 1.0
+    g[0].output, g[0].output_grad, g[0].input_grad = (ctypes.c_void_p(0x3000), ctypes.c_void_p(0x4000),
+                                                      ctypes.c_void_p(0x5000))
+    targets = (ctypes.c_void_p * 1)(0x6000)
+    loss = ctypes.c_void_p(0x7000)
+    ws = ctypes.c_void_p(0x100000)
+    assert lib.ngt_raymarch_fwd_l2_bwd_batch(g, targets, 1, 3, loss, 0, ws, 1 << 30, None) == L.NGT_ERR_INVALID_ARGUMENT
+    assert b"loss_channels" in lib.ngt_last_error_message()
+    nulls = (ctypes.c_void_p * 1)(None)
+    assert lib.ngt_raymarch_fwd_l2_bwd_batch(g, nulls, 1, 1, loss, 0, ws, 1 << 30, None) == L.NGT_ERR_INVALID_ARGUMENT
+    a.emission_channels = 0
+    assert lib.ngt_raymarch_fwd_l2_bwd_batch(g, targets, 1, 1, loss, 0, ws, 1 << 30, None) == L.NGT_ERR_UNSUPPORTED
