@@ -412,7 +412,7 @@ typedef struct {
   void* vel_y_grad;
   void* vel_z_grad;
   int32_t grad_mode;
-  int32_t deterministic;      /* exact mode: gather form, bit-reproducible gradients */
+  int32_t deterministic;      /* exact mode: 64-bit fixed-point trace adjoints, bit-reproducible gradients */
   void* workspace;
   size_t workspace_bytes;
   /* Exact, non-deterministic mode: nonzero adds the data and velocity

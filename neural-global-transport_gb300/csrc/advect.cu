@@ -140,7 +140,7 @@ struct McParams {
   CT<T>* glut;         // workspace: gradient w.r.t. the lookup (3 per cell)
   CT<T>* buf;          // reference mode: unnormalised scatter
   unsigned* cnt;       // reference mode: sample counts
-  CT<T>* gback;        // deterministic mode: back-trace gradient per cell (gathered afterwards)
+  CT<T>* gback;        // deterministic mode: back-trace gradient per cell (scattered in fixed point afterwards)
   CT<T>* gface[3];     // density, non-deterministic: face gradients accumulated by backward 2
   uint8_t* mask;       // MC_SMOOTH revert mask: written by forward 2, read by backward 1 (optional)
   CT<T>* ext;          // MC_SMOOTH: the forward trace's corner extrema (min, max per cell and channel),
@@ -150,7 +150,7 @@ struct McParams {
   Dims d;
   int order, clamp, bm, reference;
   int accumulate;      // add (atomically) the direct data gradient instead of writing it
-  int det;             // deterministic: no scatter here, the gather form follows
+  int det;             // deterministic: no float scatter here, the fixed-point scatter follows
 };
 
 __device__ __forceinline__ void cell_of(int64_t i, const Dims& d, int& x, int& y, int& z) {
@@ -506,8 +506,8 @@ __global__ void __launch_bounds__(kTileX * kTileY, 5)
   if (!ok) mbar_wait_bounded(&bar, 0, kBrickWaitPolls);  // the copy may still be landing in the brick
 }
 
-// gather sources of the deterministic form: the back-trace (value gback at
-// idx - lut) and the forward trace (value gfwd at idx + lut)
+// sample sources of the deterministic (fixed-point) adjoint: the back-trace
+// (value gback at idx - lut) and the forward trace (value gfwd at idx + lut)
 template <int C, class T, class LK>
 struct TraceSource {
   const CT<T>* val;
@@ -924,10 +924,10 @@ int launch_bwd12(McParams<T>& p, const LK& lk, cudaStream_t st) {
   const CellLaunch l = cell_launch(p.d);
   k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
   if (p.det && p.order == 2)
-    gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st);
+    fixed_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st);
   if (p.reference && p.order == 2) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gfwd, p.buf, p.cnt, n);
   k_mc_bwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
-  if (p.det) gather_adjoint<C, S>(TraceSource<C, T, LK>{p.gfwd, lk, p.d, +1}, n, p.d, p.bm, p.cnt, p.gdata, 1, st);
+  if (p.det) fixed_adjoint<C, S>(TraceSource<C, T, LK>{p.gfwd, lk, p.d, +1}, n, p.d, p.bm, p.cnt, p.gdata, 1, st);
   if (p.reference) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gdata, p.buf, p.cnt, n);
   return NGT_OK;
 }
@@ -994,7 +994,9 @@ int density_bwd(const ngt_advect_grad_args* g, cudaStream_t st) {
   } else if (p.det) {
     p.gback = reinterpret_cast<S*>(w);
     w += size_t(n) * C * sizeof(S);
-    p.cnt = reinterpret_cast<unsigned*>(w);  // gather work area
+    // the fixed-point sums (64-bit: 8-byte aligned; the workspace size allows for it)
+    w = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(w) + 15) & ~uintptr_t(15));
+    p.cnt = reinterpret_cast<unsigned*>(w);
   }
   const bool faces = g->vel_x_grad && g->vel_y_grad && g->vel_z_grad;
   if (faces && !p.det) {
@@ -1350,7 +1352,7 @@ extern "C" size_t ngt_advect_maccormack_bwd_workspace_bytes(const ngt_advect_gra
   size_t bytes = size_t(n) * size_t(C + 3) * cs;
   if (g->grad_mode == NGT_GRAD_REFERENCE) bytes += size_t(n) * (size_t(C) * cs + sizeof(unsigned));
   else if (g->deterministic)
-    bytes += size_t(n) * size_t(C) * cs + gather_bytes(n, cells_of(g->fwd.grid_dhw), g->fwd.boundary) + 256;
+    bytes += size_t(n) * size_t(C) * cs + fixed_bytes(cells_of(g->fwd.grid_dhw), int(C)) + 16;
   return bytes;
 }
 

@@ -11,6 +11,8 @@
 // its C-channel value; it returns false for samples that contribute nothing.
 #pragma once
 
+#include <algorithm>
+
 #include "ngt_common.cuh"
 
 namespace ngt {
@@ -272,6 +274,109 @@ __host__ inline void gather_adjoint(const SRC& src, int64_t nsamples, const Dims
                                                                                             nk);
   k_gather_sum<C, S, SRC><<<unsigned((d.count() + kGatherBlock - 1) / kGatherBlock), kGatherBlock, 0, st>>>(
       src, d, bm, w.offset, w.count, w.list, grad, accumulate);
+}
+
+// ------------------------------------------------------------ fixed-point form
+// The same adjoint as a scatter whose sums do not depend on the order of the
+// additions: every contribution g * w is rounded to an integer at the scale 2^E
+// and added with a 64-bit integer atomic (integer addition is associative), and a
+// last pass converts the sums.  A first pass takes the largest |value| of the
+// samples, g_max < 2^eg; a sample's corner weights to one cell sum to at most 1,
+// so no cell's sum passes nsamples * g_max, and E = 62 - eg - en with
+// nsamples <= 2^en keeps it below 2^62 while resolving each contribution to
+// 2^(en - 62) of g_max.  One pass over the samples, against the counting sort's
+// count, scan, fill and sort and a sum that sets every sample up again for each
+// of its eight corner cells.  A value that is not finite makes every cell of the
+// result NaN (the float scatter would spread it to some).
+
+__host__ inline size_t fixed_bytes(const Dims& d, int C) { return size_t(d.count()) * size_t(C) * 8 + 256; }
+
+__device__ __forceinline__ int fixed_exponent(unsigned gmax_bits, int64_t nsamples) {
+  const float g = __uint_as_float(gmax_bits);
+  if (!(g > 0.0f)) return 0;
+  int eg;
+  frexpf(g, &eg);  // g = m * 2^eg, m in [0.5, 1): every |value| (rounded to float: at most g) is below 2^eg
+  const unsigned long long n = (unsigned long long)(nsamples > 1 ? nsamples : 1);
+  const int en = n > 1 ? 64 - __clzll(n - 1) : 0;
+  return 62 - eg - en;
+}
+
+// A contribution at the scale 2^e as an integer, and back, in the data's own
+// arithmetic: float data never goes through double (slow on this GPU), and the
+// float scaling by a power of two is exact, so the integer is the one a double
+// evaluation would give.
+__device__ __forceinline__ long long fixed_of(float v, int e) { return __float2ll_rn(ldexpf(v, e)); }
+__device__ __forceinline__ long long fixed_of(double v, int e) { return __double2ll_rn(ldexp(v, e)); }
+__device__ __forceinline__ void fixed_value(long long q, int e, float& v) { v = ldexpf(__ll2float_rn(q), -e); }
+__device__ __forceinline__ void fixed_value(long long q, int e, double& v) { v = ldexp(__ll2double_rn(q), -e); }
+
+template <int C, class S, class SRC>
+__global__ void __launch_bounds__(kGatherBlock) k_fixed_max(SRC src, int64_t nsamples, unsigned* __restrict__ gmax) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  unsigned m = 0u;  // bits of |value| as float: ordered as integers, NaN and inf above every finite value
+  S p[3], g[C];
+  if (s < nsamples && src(s, p, g)) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) m = max(m, __float_as_uint(fabsf(float(g[c]))));
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(gmax, m);
+}
+
+template <int C, class S, class SRC>
+__global__ void __launch_bounds__(kGatherBlock) k_fixed_scatter(SRC src, int64_t nsamples, Dims d, int bm,
+                                                                const unsigned* __restrict__ gmax,
+                                                                unsigned long long* __restrict__ fix) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= nsamples) return;
+  const unsigned gb = *gmax;
+  if (gb == 0u || gb >= 0x7f800000u) return;  // all zero, or not finite
+  const int e = fixed_exponent(gb, nsamples);
+  S p[3], g[C];
+  if (!src(s, p, g)) return;
+  const Tri<S> t = tri_setup(p[0], p[1], p[2], d, bm);
+  if (bm == BORDER && !t.inside) return;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    bool valid;
+    const int64_t idx = tri_corner(t, q, d, valid);
+    if (!valid) continue;
+    const S w = tri_weight(t, q);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const long long v = fixed_of(mul_rn(g[c], w), e);
+      if (v) atomicAdd(fix + idx * C + c, (unsigned long long)v);
+    }
+  }
+}
+
+template <class S>
+__global__ void k_fixed_convert(const unsigned long long* __restrict__ fix, const unsigned* __restrict__ gmax,
+                                int64_t nsamples, S* __restrict__ grad, int64_t n, int accumulate) {
+  const unsigned gb = *gmax;
+  const int e = fixed_exponent(gb, nsamples);
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    S v;
+    fixed_value((long long)fix[i], e, v);
+    if (gb >= 0x7f800000u) v = S(NAN);
+    grad[i] = accumulate ? add_rn(grad[i], v) : v;
+  }
+}
+
+// Enqueue the fixed-point deterministic adjoint: grad (+)= the samples' scatter.
+// ``ws``: fixed_bytes(d, C) bytes, 8-byte aligned.
+template <int C, class S, class SRC>
+__host__ inline void fixed_adjoint(const SRC& src, int64_t nsamples, const Dims& d, int bm, void* ws, S* grad,
+                                   int accumulate, cudaStream_t st) {
+  unsigned long long* fix = static_cast<unsigned long long*>(ws);
+  unsigned* gmax = reinterpret_cast<unsigned*>(fix + d.count() * C);
+  cudaMemsetAsync(ws, 0, fixed_bytes(d, C), st);
+  const unsigned gs = unsigned((nsamples + kGatherBlock - 1) / kGatherBlock);
+  k_fixed_max<C, S, SRC><<<gs, kGatherBlock, 0, st>>>(src, nsamples, gmax);
+  k_fixed_scatter<C, S, SRC><<<gs, kGatherBlock, 0, st>>>(src, nsamples, d, bm, gmax, fix);
+  const int64_t n = d.count() * C;
+  const unsigned nb = unsigned(std::min<int64_t>((n + 255) / 256, 152 * 16));
+  k_fixed_convert<S><<<nb, 256, 0, st>>>(fix, gmax, nsamples, grad, n, accumulate);
 }
 
 }  // namespace

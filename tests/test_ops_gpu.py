@@ -686,6 +686,41 @@ def test_advect_backward_deterministic(bm):
         assert rel(r, N(t)) < 1e-4
 
 
+@pytest.mark.parametrize("C,dtype,order,clamp", [(2, np.float32, 2, "MC_SMOOTH"), (4, np.float32, 2, "NONE"),
+                                                  (1, np.float64, 2, "MC_SMOOTH"), (1, np.float32, 1, "NEGATIVE")])
+def test_advect_backward_deterministic_channels(C, dtype, order, clamp):
+    """The deterministic MacCormack adjoint (64-bit fixed-point sums of both trace
+    adjoints) with several channels, double storage and first order: the same
+    bits on every run, the oracle's gradients (f64 at 1e-10: each contribution is
+    resolved to 2^(en - 62) of the largest), and a NaN in the upstream gradient
+    reaching the gradients."""
+    from ngt_gb300 import advect, ops
+    rho, ux, uy, uz = advect_inputs(shape=(9, 11, 13), seed=31, dtype=dtype)
+    rho = np.concatenate([rho * dtype(k + 1) for k in range(C)], -1)
+    g = RNG.standard_normal(rho.shape).astype(dtype)
+    td = torch.float64 if dtype == np.float64 else torch.float32
+
+    def run(gup):
+        ts = [T(a, td).requires_grad_() for a in (rho, ux, uy, uz)]
+        ops.set_deterministic(True)
+        try:
+            y = advect.warp(*ts, order=order, clamp=clamp, boundary="CLAMP")
+            y.backward(T(gup, td))
+        finally:
+            ops.set_deterministic(False)
+        return [t.grad for t in ts]
+
+    a, b = run(g), run(g)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    ref = oadvect.density_maccormack_grad(rho, ux, uy, uz, g, order=order, clamp=clamp, boundary="CLAMP")
+    for t, r in zip(a, ref):
+        assert rel(r, N(t)) < (1e-10 if dtype == np.float64 else 1e-4)
+    gn = g.copy()
+    gn[4, 5, 6, 0] = np.nan
+    assert all(bool(torch.isnan(t).any()) for t in run(gn)[:1])
+
+
 @pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
 @pytest.mark.parametrize("C", [1, 2, 4])
 def test_advect_stored_extrema_bitexact(bm, C):
