@@ -56,6 +56,16 @@ __device__ __forceinline__ __half from_compute<__half>(float v) { return __float
 
 template <class S> __device__ __forceinline__ void atomic_add(S* p, S v) { atomicAdd(p, v); }
 
+// ------------------------------------------------------ fixed-point sums
+// A value at the scale 2^e as a 64-bit integer (for order-independent integer
+// atomic sums), and an integer sum back, in the data's own arithmetic: float data
+// never goes through double (slow on this GPU); scaling by a power of two is
+// exact, so the integer is the one a double evaluation would give.
+__device__ __forceinline__ long long fixed_of(float v, int e) { return __float2ll_rn(ldexpf(v, e)); }
+__device__ __forceinline__ long long fixed_of(double v, int e) { return __double2ll_rn(ldexp(v, e)); }
+__device__ __forceinline__ void fixed_value(long long q, int e, float& v) { v = ldexpf(__ll2float_rn(q), -e); }
+__device__ __forceinline__ void fixed_value(long long q, int e, double& v) { v = ldexp(__ll2double_rn(q), -e); }
+
 // --------------------------------------------------------------- grid dims
 struct Dims {
   int x, y, z;  // W, H, D

@@ -301,15 +301,6 @@ __device__ __forceinline__ int fixed_exponent(unsigned gmax_bits, int64_t nsampl
   return 62 - eg - en;
 }
 
-// A contribution at the scale 2^e as an integer, and back, in the data's own
-// arithmetic: float data never goes through double (slow on this GPU), and the
-// float scaling by a power of two is exact, so the integer is the one a double
-// evaluation would give.
-__device__ __forceinline__ long long fixed_of(float v, int e) { return __float2ll_rn(ldexpf(v, e)); }
-__device__ __forceinline__ long long fixed_of(double v, int e) { return __double2ll_rn(ldexp(v, e)); }
-__device__ __forceinline__ void fixed_value(long long q, int e, float& v) { v = ldexpf(__ll2float_rn(q), -e); }
-__device__ __forceinline__ void fixed_value(long long q, int e, double& v) { v = ldexp(__ll2double_rn(q), -e); }
-
 template <int C, class S, class SRC>
 __global__ void __launch_bounds__(kGatherBlock) k_fixed_max(SRC src, int64_t nsamples, unsigned* __restrict__ gmax) {
   const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;

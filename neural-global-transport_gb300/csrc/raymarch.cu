@@ -211,7 +211,8 @@ __global__ void k_fix_convert(const unsigned long long* __restrict__ fix, const 
                               S* __restrict__ grad, int64_t n, int accumulate) {
   const int e = fix_exponent(fst, rays);
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-    const S v = S(ldexp(double((long long)fix[i]), -e));
+    S v;
+    fixed_value((long long)fix[i], e, v);  // in the compute type: float data never goes through double
     grad[i] = accumulate ? grad[i] + v : v;
   }
 }
@@ -837,8 +838,14 @@ int raymarch_bwd_impl(const ngt_raymarch_grad_args* a, const FusedLoss* fl, void
   build_cams(p, &a->fwd, w + l.cams, st);
 
   if (a->grad_mode == NGT_GRAD_EXACT && a->deterministic) {
-    // statistics pass, fixed-point scatter pass, conversion (direct gathers, no quad layout)
+    // statistics pass, fixed-point scatter pass, conversion; the samples are read
+    // through the caller's prepared quad layout when there is one (the same values
+    // as the direct gathers, two vector loads instead of eight), else directly
     const bool bl = needs_sign_flag(a);
+    if (quad_case(&a->fwd) && a->fwd.quad) {
+      p.quad = static_cast<const char*>(a->fwd.quad) + kQuadHeader;
+      p.qd = QuadDims::of(p.din);
+    }
     p.fst = reinterpret_cast<FixStats*>(w + l.fst);
     p.fix = reinterpret_cast<unsigned long long*>(w + l.fix);
     p.nrays = int64_t(num_slots(p)) * p.H * p.W;

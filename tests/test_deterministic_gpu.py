@@ -117,3 +117,48 @@ def test_autograd_deterministic_flag():
         assert torch.equal(grads[0], grads[1])
     finally:
         ops.set_deterministic(old)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("boundary", ["BORDER", "CLAMP", "WRAP"])
+def test_raymarch_deterministic_prepared_quad(dtype, boundary):
+    """The deterministic render adjoint reads its samples through the caller's
+    prepared quad layout when there is one: the same bits as with the direct
+    gathers (the quad reads the same corner values and weights)."""
+    import ctypes
+    from ngt_gb300 import _lib as L
+    from ngt_gb300 import ops, scene
+    lib = L.load()
+    vol, cam = (10, 13, 15), (12, 14, 16)
+    rng = np.random.default_rng(7)
+    x = torch.as_tensor(rng.uniform(0, 0.5, (1,) + vol + (1,)).astype(np.float32), device="cuda").to(dtype)
+    cams = scene.orbit_cameras(list(cam), [25.0, -70.0])
+    M = scene.model_params([scene.volume_transform(list(vol))])
+    V, P, F = scene.camera_params(cams)
+    mats = [ops._floats(m, w, x.device) for m, w in ((M, 16), (V, 16), (P, 16), (F, 6))]
+    attrs = dict(interpolation="LINEAR", boundary=boundary, blending_mode="BEER_LAMBERT", keep_dims=False,
+                 separate_camera_batch=True, emission_scale=(0.8, 1.3))
+    y = torch.empty((1, 2) + cam[1:] + (2,), device="cuda")
+    r = ops._ray_args(x, *mats, list(cam), y, attrs)
+    st = ops._stream()
+    assert lib.ngt_raymarch_fwd(ctypes.byref(r), st) == L.NGT_OK
+    gy = torch.as_tensor(rng.standard_normal(tuple(y.shape)).astype(np.float32), device="cuda")
+    quad = torch.empty(int(lib.ngt_raymarch_quad_bytes(ctypes.byref(r))), dtype=torch.uint8, device="cuda")
+    out = []
+    for prepared in (False, True):
+        if prepared:
+            assert lib.ngt_raymarch_quad(ctypes.byref(r), ops._ptr(quad), st) == L.NGT_OK
+            r.quad = ops._ptr(quad)
+        g = L.RaymarchGradArgs()
+        g.fwd = r
+        gx = torch.empty(x.shape, device="cuda")
+        g.output, g.output_grad, g.input_grad = ops._ptr(y), ops._ptr(gy), ops._ptr(gx)
+        g.grad_mode, g.deterministic = L.GRAD["exact"], 1
+        ws = torch.empty(int(lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(g))), dtype=torch.uint8,
+                         device="cuda")
+        g.workspace, g.workspace_bytes = ops._ptr(ws), ws.numel()
+        assert lib.ngt_raymarch_bwd(ctypes.byref(g), st) == L.NGT_OK
+        torch.cuda.synchronize()
+        out.append(gx)
+    assert float(out[0].abs().max()) > 0
+    assert torch.equal(out[0], out[1])
