@@ -274,8 +274,9 @@ typedef struct {
    * below 2^62, so no sum overflows and each contribution is resolved to
    * 2^-36 of the largest at 2^26 samples), the integers are summed with
    * integer atomics (associative: the same sums in every run) and converted
-   * once.  Direct gathers, two extra passes over the rays; the workspace holds
-   * one 64-bit integer per input cell and channel. */
+   * once.  Samples read through fwd.quad when one is prepared (the same
+   * values), else gathered directly; two passes over the rays; the workspace
+   * holds one 64-bit integer per input cell and channel. */
   int32_t deterministic;
 } ngt_raymarch_grad_args;
 
