@@ -471,6 +471,9 @@ typedef struct {
   int32_t grad_mode;
   void* workspace;
   size_t workspace_bytes;
+  /* Exact mode: nonzero takes each component's trace adjoints as 64-bit
+   * fixed-point sums (bit-reproducible gradients, as for the density). */
+  int32_t deterministic;
 } ngt_advect_velocity_grad_args;
 
 int ngt_advect_velocity_fwd(const ngt_advect_velocity_args* args, void* stream);

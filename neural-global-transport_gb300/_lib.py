@@ -106,7 +106,7 @@ class AdvectVelocityArgs(ctypes.Structure):
 class AdvectVelocityGradArgs(ctypes.Structure):
     _fields_ = [("fwd", AdvectVelocityArgs), ("grad_x", c_vp), ("grad_y", c_vp), ("grad_z", c_vp),
                 ("vel_x_grad", c_vp), ("vel_y_grad", c_vp), ("vel_z_grad", c_vp), ("grad_mode", c_i32),
-                ("workspace", c_vp), ("workspace_bytes", c_sz)]
+                ("workspace", c_vp), ("workspace_bytes", c_sz), ("deterministic", c_i32)]
 
 
 # name -> (argument types, result type)

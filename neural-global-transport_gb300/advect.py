@@ -184,7 +184,7 @@ class _WarpVelocity(torch.autograd.Function):
                ctypes.byref(_vel_args(vx, vy, vz, outs, fwds, dt, order, clamp, boundary, scratch)), _stream())
         ctx.save_for_backward(vx, vy, vz, *[f for f in fwds if f is not None])
         ctx.scratch = scratch
-        ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode())
+        ctx.cfg = (dt, order, clamp, boundary, get_gradient_mode(), get_deterministic())
         return tuple(outs)
 
     @staticmethod
@@ -192,7 +192,7 @@ class _WarpVelocity(torch.autograd.Function):
         saved = ctx.saved_tensors
         vx, vy, vz = saved[:3]
         fwds = list(saved[3:]) if len(saved) > 3 else [None, None, None]
-        dt, order, clamp, boundary, mode = ctx.cfg
+        dt, order, clamp, boundary, mode, det = ctx.cfg
         cd = compute_dtype(vx)
         gs = [(g if g is not None else torch.zeros(t.shape, device=t.device)).to(cd).contiguous()
               for g, t in zip((gx, gy, gz), (vx, vy, vz))]
@@ -202,6 +202,7 @@ class _WarpVelocity(torch.autograd.Function):
         g.grad_x, g.grad_y, g.grad_z = (_ptr(t) for t in gs)
         g.vel_x_grad, g.vel_y_grad, g.vel_z_grad = (_ptr(t) for t in outs)
         g.grad_mode = L.GRAD[mode]
+        g.deterministic = int(bool(det) and mode == "exact")
         ws = _workspace(L.load().ngt_advect_velocity_bwd_workspace_bytes(ctypes.byref(g)), vx.device)
         g.workspace, g.workspace_bytes = _ptr(ws), ws.numel()
         L.call("ngt_advect_velocity_bwd", ctypes.byref(g), _stream())

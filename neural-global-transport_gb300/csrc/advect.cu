@@ -1130,6 +1130,7 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
   const ngt_advect_velocity_args* a = &g->fwd;
   const Dims cells = cells_of(a->grid_dhw);
   const int reference = g->grad_mode == NGT_GRAD_REFERENCE;
+  const int det = !reference && g->deterministic;
   const int64_t nmax = max_faces(a->grid_dhw), nall = all_faces(a->grid_dhw);
   char* w = static_cast<char*>(g->workspace);
   S* gfwd = reinterpret_cast<S*>(w);
@@ -1143,9 +1144,16 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
   S* glut = gluts[0];
   S* buf = nullptr;
   unsigned* cnt = nullptr;
+  S* gback = nullptr;
   if (reference) {
     buf = reinterpret_cast<S*>(w);
     w += size_t(nall) * sizeof(S);
+    cnt = reinterpret_cast<unsigned*>(w);
+  } else if (det) {
+    // the back-trace gradient, then the fixed-point sums (8-byte aligned)
+    gback = reinterpret_cast<S*>(w);
+    w += size_t(nmax) * sizeof(S);
+    w = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(w) + 15) & ~uintptr_t(15));
     cnt = reinterpret_cast<unsigned*>(w);
   }
   S* gu[3] = {static_cast<S*>(g->vel_x_grad), static_cast<S*>(g->vel_y_grad), static_cast<S*>(g->vel_z_grad)};
@@ -1160,8 +1168,13 @@ int vel_bwd(const ngt_advect_velocity_grad_args* g, cudaStream_t st) {
     p.gfwd = gfwd;
     p.glut = reference ? glut : gluts[c];
     p.reference = reference;
+    p.det = det;
+    p.gback = gback;
     p.buf = buf;
     p.cnt = cnt;
+    // added to the zeroed face gradients (the lookup adjoint adds the rest); in the
+    // deterministic mode each cell's direct term is its only addition there before
+    // the fixed-point sums, so the result does not depend on any order
     p.accumulate = 1;
     int rc = a->lookup[c]
                  ? launch_bwd12<1, T>(p, StoredLookup<T>{static_cast<const CT<T>*>(a->lookup[c]), p.d}, st)
@@ -1404,6 +1417,8 @@ extern "C" size_t ngt_advect_velocity_bwd_workspace_bytes(const ngt_advect_veloc
   const bool reference = g->grad_mode == NGT_GRAD_REFERENCE;
   size_t bytes = size_t(max_faces(g->fwd.grid_dhw)) * (reference ? 4 : 10) * cs;
   if (reference) bytes += size_t(all_faces(g->fwd.grid_dhw)) * (cs + sizeof(unsigned));
+  else if (g->deterministic)  // back-trace gradient and the fixed-point sums of the largest component lattice
+    bytes += size_t(max_faces(g->fwd.grid_dhw)) * (cs + 8) + 256 + 16;
   return bytes;
 }
 

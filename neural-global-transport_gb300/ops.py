@@ -28,8 +28,8 @@ _DETERMINISTIC = [False]
 
 def set_deterministic(flag):
     """Bit-reproducible input gradients in exact mode: the gather form for the
-    LUT and transform resamples and the advection, fixed-point integer
-    accumulation for the raymarch."""
+    LUT and transform resamples, fixed-point integer accumulation for the
+    advection of density and velocity and for the raymarch."""
     _DETERMINISTIC[0] = bool(flag)
 
 

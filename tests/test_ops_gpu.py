@@ -617,6 +617,32 @@ def test_velocity_advect_forward_bitexact(bm, order, clamp):
 
 
 @pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
+@pytest.mark.parametrize("order,clamp", [(2, "MC_SMOOTH"), (1, "NONE")])
+def test_velocity_advect_backward_deterministic(bm, order, clamp):
+    """Velocity self-advection with the deterministic adjoint (fixed-point trace
+    adjoints per face component): the same bits on every run and the oracle's
+    gradients."""
+    from ngt_gb300 import advect, ops
+    _, ux, uy, uz = advect_inputs(shape=(9, 10, 11), seed=41)
+    gs = [RNG.standard_normal(u.shape).astype(np.float32) for u in (ux, uy, uz)]
+    runs = []
+    for _ in range(2):
+        ts = [T(u).requires_grad_() for u in (ux, uy, uz)]
+        ops.set_deterministic(True)
+        try:
+            out = advect.warp_velocity(*ts, order=order, clamp=clamp, boundary=bm)
+            torch.autograd.backward(out, [T(g) for g in gs])
+        finally:
+            ops.set_deterministic(False)
+        runs.append([t.grad for t in ts])
+    for a, b in zip(*runs):
+        assert torch.equal(a, b)
+    ref = oadvect.velocity_maccormack_grad(ux, uy, uz, gs, order=order, clamp=clamp, boundary=bm)
+    for t, r in zip(runs[0], ref):
+        assert rel(r, N(t)) < 1e-4
+
+
+@pytest.mark.parametrize("bm", ["CLAMP", "BORDER", "WRAP"])
 @pytest.mark.parametrize("mode", ["exact", "reference"])
 def test_velocity_advect_backward(bm, mode):
     from ngt_gb300 import advect, ops
