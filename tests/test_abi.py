@@ -515,3 +515,30 @@ def test_fused_batch_validation(lib):
     assert lib.ngt_raymarch_fwd_l2_bwd_batch(g, nulls, 1, 1, loss, 0, ws, 1 << 30, None) == L.NGT_ERR_INVALID_ARGUMENT
     a.emission_channels = 0
     assert lib.ngt_raymarch_fwd_l2_bwd_batch(g, targets, 1, 1, loss, 0, ws, 1 << 30, None) == L.NGT_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("C", [1, 2, 4])
+def test_deterministic_advection_workspace_covers_fixed_point(lib, C):
+    """The deterministic advection backward's workspace holds the fwd-field and
+    lookup gradients, the back-trace gradient and the 64-bit fixed-point sums
+    (one per cell and channel) after 16-byte alignment; the velocity one the
+    same over its largest face lattice."""
+    from ngt_gb300 import _lib as L
+    D, H, W = 5, 7, 9
+    n = D * H * W
+    g = L.AdvectGradArgs()
+    g.fwd.dtype, g.fwd.grid_dhw, g.fwd.channels = L.F32, L.I64x3(D, H, W), C
+    g.grad_mode = L.GRAD["exact"]
+    exact = int(lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g)))
+    g.deterministic = 1
+    det = int(lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(g)))
+    assert exact == n * (C + 3) * 4
+    assert det >= exact + n * C * 4 + 15 + n * C * 8 + 4
+    v = L.AdvectVelocityGradArgs()
+    v.fwd.dtype, v.fwd.grid_dhw = L.F32, L.I64x3(D, H, W)
+    v.grad_mode = L.GRAD["exact"]
+    vexact = int(lib.ngt_advect_velocity_bwd_workspace_bytes(ctypes.byref(v)))
+    v.deterministic = 1
+    vdet = int(lib.ngt_advect_velocity_bwd_workspace_bytes(ctypes.byref(v)))
+    nmax = max((W + 1) * H * D, W * (H + 1) * D, W * H * (D + 1))
+    assert vdet >= vexact + nmax * 4 + 15 + nmax * 8 + 4
