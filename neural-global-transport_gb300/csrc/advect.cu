@@ -923,11 +923,16 @@ int launch_bwd12(McParams<T>& p, const LK& lk, cudaStream_t st) {
   const unsigned nb = ceil_div_u(n, kBlock);
   const CellLaunch l = cell_launch(p.d);
   k_mc_bwd1<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
-  if (p.det && p.order == 2)
-    fixed_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st);
+  if (p.det && p.order == 2 &&
+      fixed_adjoint<C, S>(TraceSource<C, T, LK>{p.gback, lk, p.d, -1}, n, p.d, p.bm, p.cnt, p.gfwd, 1, st) !=
+          cudaSuccess)
+    return check_launch("advect_bwd memset");
   if (p.reference && p.order == 2) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gfwd, p.buf, p.cnt, n);
   k_mc_bwd2<C, T, LK><<<l.grid, l.block, 0, st>>>(p, lk);
-  if (p.det) fixed_adjoint<C, S>(TraceSource<C, T, LK>{p.gfwd, lk, p.d, +1}, n, p.d, p.bm, p.cnt, p.gdata, 1, st);
+  if (p.det &&
+      fixed_adjoint<C, S>(TraceSource<C, T, LK>{p.gfwd, lk, p.d, +1}, n, p.d, p.bm, p.cnt, p.gdata, 1, st) !=
+          cudaSuccess)
+    return check_launch("advect_bwd memset");
   if (p.reference) k_norm_add<C, S><<<nb, kBlock, 0, st>>>(p.gdata, p.buf, p.cnt, n);
   return NGT_OK;
 }

@@ -256,14 +256,17 @@ __host__ inline GatherWork gather_layout(void* ws, int64_t nsamples, const Dims&
 }
 
 // Enqueue the full deterministic adjoint: grad (+)= gather of the sources' samples.
+// Returns the status of the enqueueing (the launches' own errors surface in the
+// caller's launch check).
 template <int C, class S, class SRC>
-__host__ inline void gather_adjoint(const SRC& src, int64_t nsamples, const Dims& d, int bm, void* ws, S* grad,
-                                    int accumulate, cudaStream_t st) {
+__host__ inline cudaError_t gather_adjoint(const SRC& src, int64_t nsamples, const Dims& d, int bm, void* ws, S* grad,
+                                           int accumulate, cudaStream_t st) {
   const int64_t nk = key_count(d, bm);
   const int64_t nb = (nk + kScanBlock - 1) / kScanBlock;
   GatherWork w = gather_layout(ws, nsamples, d, bm);
-  cudaMemsetAsync(w.count, 0, size_t(nk) * sizeof(int), st);
-  cudaMemsetAsync(w.cursor, 0, size_t(nk) * sizeof(int), st);
+  cudaError_t e = cudaMemsetAsync(w.count, 0, size_t(nk) * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.cursor, 0, size_t(nk) * sizeof(int), st);
+  if (e != cudaSuccess) return e;
   const unsigned gs = unsigned((nsamples + kGatherBlock - 1) / kGatherBlock);
   k_gather_count<C, S, SRC><<<gs, kGatherBlock, 0, st>>>(src, nsamples, d, bm, w.keys, w.count);
   k_scan_blocks<<<unsigned(nb), kScanBlock, 0, st>>>(w.count, w.offset, w.sums, nk);
@@ -274,6 +277,7 @@ __host__ inline void gather_adjoint(const SRC& src, int64_t nsamples, const Dims
                                                                                             nk);
   k_gather_sum<C, S, SRC><<<unsigned((d.count() + kGatherBlock - 1) / kGatherBlock), kGatherBlock, 0, st>>>(
       src, d, bm, w.offset, w.count, w.list, grad, accumulate);
+  return cudaSuccess;
 }
 
 // ------------------------------------------------------------ fixed-point form
@@ -355,19 +359,22 @@ __global__ void k_fixed_convert(const unsigned long long* __restrict__ fix, cons
 }
 
 // Enqueue the fixed-point deterministic adjoint: grad (+)= the samples' scatter.
-// ``ws``: fixed_bytes(d, C) bytes, 8-byte aligned.
+// ``ws``: fixed_bytes(d, C) bytes, 8-byte aligned.  Returns the status of the
+// enqueueing (the launches' own errors surface in the caller's launch check).
 template <int C, class S, class SRC>
-__host__ inline void fixed_adjoint(const SRC& src, int64_t nsamples, const Dims& d, int bm, void* ws, S* grad,
-                                   int accumulate, cudaStream_t st) {
+__host__ inline cudaError_t fixed_adjoint(const SRC& src, int64_t nsamples, const Dims& d, int bm, void* ws, S* grad,
+                                          int accumulate, cudaStream_t st) {
   unsigned long long* fix = static_cast<unsigned long long*>(ws);
   unsigned* gmax = reinterpret_cast<unsigned*>(fix + d.count() * C);
-  cudaMemsetAsync(ws, 0, fixed_bytes(d, C), st);
+  const cudaError_t e = cudaMemsetAsync(ws, 0, fixed_bytes(d, C), st);
+  if (e != cudaSuccess) return e;
   const unsigned gs = unsigned((nsamples + kGatherBlock - 1) / kGatherBlock);
   k_fixed_max<C, S, SRC><<<gs, kGatherBlock, 0, st>>>(src, nsamples, gmax);
   k_fixed_scatter<C, S, SRC><<<gs, kGatherBlock, 0, st>>>(src, nsamples, d, bm, gmax, fix);
   const int64_t n = d.count() * C;
   const unsigned nb = unsigned(std::min<int64_t>((n + 255) / 256, 152 * 16));
   k_fixed_convert<S><<<nb, 256, 0, st>>>(fix, gmax, nsamples, grad, n, accumulate);
+  return cudaSuccess;
 }
 
 }  // namespace

@@ -607,9 +607,11 @@ int lut_bwd_typed(const ngt_sample_lut_grad_args* a, cudaStream_t st) {
     const int64_t ns = (p.sep ? int64_t(p.V) : 1) * p.dout.count();
     for (int b = 0; b < p.N; ++b) {
       T* ig = p.in_grad + int64_t(b) * vsz * C;
-      if (C == 1) gather_adjoint<1, T>(LutSource<1, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
-      else if (C == 2) gather_adjoint<2, T>(LutSource<2, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
-      else gather_adjoint<4, T>(LutSource<4, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
+      cudaError_t e;
+      if (C == 1) e = gather_adjoint<1, T>(LutSource<1, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
+      else if (C == 2) e = gather_adjoint<2, T>(LutSource<2, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
+      else e = gather_adjoint<4, T>(LutSource<4, T>{p, b}, ns, p.din, p.bm, a->workspace, ig, 0, st);
+      if (e != cudaSuccess) return check_launch("sample_lut_bwd memset");
     }
   }
   if (reference) {
@@ -737,9 +739,11 @@ int xf_bwd_typed(const ngt_sample_transform_grad_args* a, cudaStream_t st) {
     const int64_t ns = xf_det_samples(&a->fwd);
     for (int b = 0; b < p.N; ++b) {
       T* ig = p.in_grad + int64_t(b) * vsz * C;
-      if (C == 1) gather_adjoint<1, T>(XfSource<1, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
-      else if (C == 2) gather_adjoint<2, T>(XfSource<2, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
-      else gather_adjoint<4, T>(XfSource<4, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
+      cudaError_t e;
+      if (C == 1) e = gather_adjoint<1, T>(XfSource<1, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
+      else if (C == 2) e = gather_adjoint<2, T>(XfSource<2, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
+      else e = gather_adjoint<4, T>(XfSource<4, T>{p, cams, b}, ns, p.din, p.bm, gw, ig, 0, st);
+      if (e != cudaSuccess) return check_launch("sample_transform_bwd memset");
     }
     return check_launch("ngt_sample_transform_bwd");
   }
