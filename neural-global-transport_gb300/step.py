@@ -248,22 +248,15 @@ class RenderAdvectStep:
 _PLANS = {}
 _MAX_PLANS = 4
 _GRAPHS_PER_PASS = 4
-_MATRIX_KEYS = collections.OrderedDict()  # ids of matrix objects -> (the objects, their content key)
 
 
 def _matrix_key(M, V, P, F):
-    """Content key of the camera matrices, memoised by object identity (the
-    objects are kept referenced with their entry, so their ids stay theirs)."""
-    ids = (id(M), id(V), id(P), id(F))
-    hit = _MATRIX_KEYS.get(ids)
-    if hit is not None and all(not isinstance(m, torch.Tensor) for m in (M, V, P, F)):
-        return hit[1]
-    key = tuple(np.ascontiguousarray(np.asarray(m.detach().cpu() if isinstance(m, torch.Tensor) else m,
-                                                np.float32)).tobytes() for m in (M, V, P, F))
-    _MATRIX_KEYS[ids] = ((M, V, P, F), key)
-    if len(_MATRIX_KEYS) > 64:
-        _MATRIX_KEYS.popitem(last=False)
-    return key
+    """Content key of the camera matrices (their float32 bytes), formed on every
+    call: matrices changed in place between calls key another step, so a step is
+    never reused with cameras it was not built for (a few microseconds for the
+    usual handful of cameras)."""
+    return tuple(np.ascontiguousarray(np.asarray(m.detach().cpu() if isinstance(m, torch.Tensor) else m,
+                                                 np.float32)).tobytes() for m in (M, V, P, F))
 
 
 def _plan_key(rho, ux, uy, uz, M, V, P, F, image_dhw, options):

@@ -87,3 +87,21 @@ def test_graph_replay_reads_current_data():
         assert abs(float(loss) - float(want_loss)) <= 1e-5 * abs(float(want_loss)), it
         for x, g in zip(xs, want):
             assert rel(x.grad, g) < 1e-4, it
+
+
+def test_cameras_changed_in_place_take_effect():
+    """Camera matrices updated in place between calls (the same array objects)
+    render with their new values: the loss is that of the operator composition
+    with the moved cameras, not a step kept for the old ones."""
+    from ngt_gb300.step import render_advect_loss
+    dev = torch.device("cuda", 0)
+    w, ts = inputs(4, dev)
+    tgt = torch.zeros((1, 2, 24, 20, 1), device=dev) + 0.01
+    M, V, P, F = (np.array(m, np.float32) for m in (w.M, w.V, w.P, w.F))
+    first = float(render_advect_loss(*ts, M, V, P, F, tgt, w.image_dhw))
+    V[:, 12:15] += np.float32(0.35)  # every camera shifted, in place
+    second = float(render_advect_loss(*ts, M, V, P, F, tgt, w.image_dhw))
+    w.M, w.V, w.P, w.F = M.copy(), V.copy(), P.copy(), F.copy()
+    want, _ = composed(ts, w, tgt)
+    assert abs(second - float(want)) <= 1e-5 * abs(float(want))
+    assert abs(second - first) > 1e-3 * abs(first)
