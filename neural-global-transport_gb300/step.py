@@ -22,7 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
-from .ops import _code, _ptr, sample_cache_pays
+from .ops import _code, _ptr, get_deterministic, sample_cache_pays
 
 
 class RenderAdvectStep:
@@ -35,7 +35,7 @@ class RenderAdvectStep:
 
     def __init__(self, rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, light=1.0, order=2,
                  clamp="MC_SMOOTH", advect_boundary="CLAMP", render_boundary="BORDER", grad_mode="exact",
-                 background=None):
+                 background=None, deterministic=False):
         dev = rho.device
         self.lib = L.load()
         self.rho, self.ux, self.uy, self.uz = rho.contiguous(), ux.contiguous(), uy.contiguous(), uz.contiguous()
@@ -95,6 +95,10 @@ class RenderAdvectStep:
         ag.output_grad, ag.data_grad = _ptr(self.g_rho_adv), _ptr(self.g_rho)
         ag.vel_x_grad, ag.vel_y_grad, ag.vel_z_grad = _ptr(self.g_ux), _ptr(self.g_uy), _ptr(self.g_uz)
         ag.grad_mode = L.GRAD[grad_mode]
+        # the bit-reproducible (fixed-point) adjoints, exact mode only; set before the
+        # workspaces are sized
+        det = int(bool(deterministic) and grad_mode == "exact")
+        ag.deterministic = det
         self.adv_ws = torch.empty(int(self.lib.ngt_advect_maccormack_bwd_workspace_bytes(ctypes.byref(ag))),
                                   dtype=torch.uint8, device=dev)
         ag.workspace, ag.workspace_bytes = _ptr(self.adv_ws), self.adv_ws.numel()
@@ -115,7 +119,7 @@ class RenderAdvectStep:
         # the render's forward and backward; with the exact backward it also keeps
         # the forward's density samples, which the one-pass adjoint reads back
         # instead of gathering them again, where that pays (ops.sample_cache_pays)
-        r.sample_cache = int(grad_mode == "exact" and sample_cache_pays((D, H, W), 1, rho.dtype, dev))
+        r.sample_cache = int(grad_mode == "exact" and not det and sample_cache_pays((D, H, W), 1, rho.dtype, dev))
         nq = int(self.lib.ngt_raymarch_quad_bytes(ctypes.byref(r)))
         self.ray_quad = torch.empty(nq, dtype=torch.uint8, device=dev) if nq else None
         if nq:
@@ -140,6 +144,7 @@ class RenderAdvectStep:
         rg.fwd = r
         rg.output, rg.output_grad, rg.input_grad = _ptr(self.image), _ptr(self.g_image), _ptr(self.g_rho_adv)
         rg.grad_mode = L.GRAD[grad_mode]
+        rg.deterministic = det
         self.ray_ws = None
         nb = int(self.lib.ngt_raymarch_bwd_workspace_bytes(ctypes.byref(rg)))
         if nb:
@@ -366,19 +371,22 @@ def render_advect_loss(rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=1.0, 
     autograd node instead of three nodes and their intermediate tensors: the
     step's buffers are kept per shape and camera set and reused by later calls,
     and its passes are replayed as CUDA graphs once the same tensor addresses
-    come back."""
+    come back.  With ``ops.set_deterministic(True)`` the gradients come from
+    the bit-reproducible adjoints (fixed-point sums), the same bits on every
+    run."""
     dev = rho.device
     rho, ux, uy, uz = (t.contiguous() for t in (rho, ux, uy, uz))
     cd = torch.float64 if rho.dtype == torch.float64 else torch.float32
     targets = torch.as_tensor(targets, device=dev).to(cd).contiguous()
     options = dict(dt=float(dt), light=float(light), order=int(order), clamp=clamp, advect_boundary=advect_boundary,
-                   render_boundary=render_boundary, background=background is not None)
+                   render_boundary=render_boundary, background=background is not None,
+                   deterministic=get_deterministic())
     key = _plan_key(rho, ux, uy, uz, M, V, P, F, image_dhw, options)
 
     def make():
         return RenderAdvectStep(rho, ux, uy, uz, M, V, P, F, targets, image_dhw, dt=dt, light=light, order=order,
                                 clamp=clamp, advect_boundary=advect_boundary, render_boundary=render_boundary,
-                                background=background)
+                                background=background, deterministic=options["deterministic"])
 
     plan = _take_plan(key, make)
     if background is not None:

@@ -105,3 +105,27 @@ def test_cameras_changed_in_place_take_effect():
     want, _ = composed(ts, w, tgt)
     assert abs(second - float(want)) <= 1e-5 * abs(float(want))
     assert abs(second - first) > 1e-3 * abs(first)
+
+
+def test_deterministic_loss_repeats_bits():
+    """With ops.set_deterministic(True) the one-node loss takes the fixed-point
+    adjoints: the same gradient bits on every call, and the operator
+    composition's gradients to the float tolerance."""
+    from ngt_gb300 import ops
+    from ngt_gb300.step import render_advect_loss
+    dev = torch.device("cuda", 0)
+    w, ts = inputs(6, dev)
+    tgt = torch.zeros((1, 2, 24, 20, 1), device=dev) + 0.01
+    _, want = composed(ts, w, tgt)
+    runs = []
+    ops.set_deterministic(True)
+    try:
+        for _ in range(2):
+            xs = [t.clone().requires_grad_() for t in ts]
+            render_advect_loss(*xs, w.M, w.V, w.P, w.F, tgt, w.image_dhw).backward()
+            runs.append([x.grad for x in xs])
+    finally:
+        ops.set_deterministic(False)
+    for a, b, g in zip(runs[0], runs[1], want):
+        assert torch.equal(a, b)
+        assert rel(a, g) < 1e-4
