@@ -83,3 +83,22 @@ def test_velocity_advection_gradient_matches_differences(bm, order, clamp):
 
     grads = oadvect.velocity_maccormack_grad(*u, gs, 1.0, order, clamp, bm)
     check(grads, f, u, gs, rng, picks=6)
+
+
+def test_background_composite_gradient_matches_differences():
+    """The background composite of the render composition (renderer.py:779-781,
+    804-806: light + background * exp(-d), the depth channel cut), restated from
+    TensorFlow ops: its adjoint to the image (light and depth channels) and to
+    the background shared by the batch, against central differences."""
+    from oracle import ops as oops
+    rng = np.random.default_rng(5)
+    image = rng.uniform(0.0, 2.0, (2, 3, 4, 5, 3))  # batch, views, H, W, [light x2, depth]
+    bkg = rng.uniform(0.0, 1.0, (3, 4, 5, 2))
+    g = rng.standard_normal((2, 3, 4, 5, 2))
+    gi, gb = oops.background_composite_grad(image, bkg, g)
+    for which, an in ((0, gi), (1, gb)):
+        arr = (image, bkg)[which]
+        for _ in range(20):
+            idx = tuple(int(rng.integers(0, n)) for n in arr.shape)
+            d = fd_entry(oops.background_composite, [image, bkg], which, idx, g)
+            assert abs(d - float(an[idx])) <= 1e-8 * max(1.0, abs(float(an[idx])))
