@@ -1,5 +1,6 @@
-"""The oracle's advection gradients against central finite differences (CPU,
-float64).
+"""The oracle's gradients of the compositions the reference forms with
+TensorFlow ops -- the advection and the background composite -- against central
+finite differences (CPU, float64).
 
 The reference forms the MacCormack warp and its gradient through TensorFlow
 (data_structures.py:1690-1737 for the density, 1081-1164 for the velocity),
