@@ -1,7 +1,8 @@
 """Known answers and adjoint identities of the oracle (CPU, float64).
 
 Known answers: an integer shift of the velocity moves the density by whole
-cells (CLAMP repeats the edge, WRAP rolls); zero velocity is the identity; a
+cells (CLAMP repeats the edge, WRAP rolls), and a uniform integer ux carries
+the velocity's other faces the same way; zero velocity is the identity; a
 constant grid blends to the closed-form Beer-Lambert sums; rays that miss the
 grid's box render 0 under BORDER; index -> object space -> index round trips.
 Adjoint identities <A x, y> = <x, A^T y> hold for every operator that is linear
@@ -74,6 +75,33 @@ def test_integer_velocity_shifts_by_whole_cells(axis, comp, shift):
     src = np.clip(np.arange(n) - shift, 0, n - 1)
     clamped = np.take(rho, src, axis=axis)
     assert np.array_equal(oadvect.density_maccormack(rho, *u, order=1, clamp="NONE", boundary="CLAMP"), clamped)
+
+
+@pytest.mark.parametrize("shift", [1, 2, 3])
+@pytest.mark.parametrize("order,clamp", [(1, "NONE"), (2, "MC_SMOOTH"), (2, "NONE")])
+def test_velocity_self_advection_integer_transport(shift, order, clamp):
+    """Self-advection (VelocityGrid.warped) under a uniform integer ux = c with
+    uy = 0 and uz varying along x only: ux stays c, uy stays 0, and the z faces
+    are carried c cells along x (their own z motion reads a field constant along
+    z).  WRAP rolls them; CLAMP repeats the edge, and second-order MacCormack's
+    back-trace from x + c, clamped at the last cell there, leaves the correction
+    0.5 * (f(x) - f(W-1-c)) on the last c cells (MC_SMOOTH may revert it: only
+    the other cells are fixed then)."""
+    D, H, W = 4, 5, 9
+    f = RNG.uniform(-0.4, 0.4, W)
+    u = (np.full((D, H, W + 1), float(shift)), np.zeros((D, H + 1, W)), np.broadcast_to(f, (D + 1, H, W)).copy())
+    ox, oy, oz = oadvect.velocity_maccormack(*u, 1.0, order, clamp, "WRAP")
+    assert np.array_equal(oz, np.broadcast_to(np.roll(f, shift), oz.shape))
+    assert np.all(ox == shift) and np.all(oy == 0)
+    ox, oy, oz = oadvect.velocity_maccormack(*u, 1.0, order, clamp, "CLAMP")
+    x = np.arange(W)
+    fwd = f[np.clip(x - shift, 0, W - 1)]
+    edge = x > W - 1 - shift if order == 2 else np.zeros(W, bool)
+    assert np.array_equal(oz[..., ~edge], np.broadcast_to(fwd[~edge], oz[..., ~edge].shape))
+    if order == 2 and clamp == "NONE":
+        want = fwd[edge] + 0.5 * (f[edge] - f[W - 1 - shift])
+        assert np.array_equal(oz[..., edge], np.broadcast_to(want, oz[..., edge].shape))
+    assert np.all(ox == shift) and np.all(oy == 0)
 
 
 @pytest.mark.parametrize("depth", [1, 5, 16])
