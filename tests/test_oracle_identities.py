@@ -62,7 +62,8 @@ def test_zero_velocity_is_identity(order, bm, clamp):
 def test_integer_velocity_shifts_by_whole_cells(axis, comp, shift):
     """dt * u = an integer number of cells: semi-Lagrangian under WRAP rolls the
     grid, under CLAMP shifts it with the edge cells repeated; MacCormack under
-    WRAP rolls it too (the back-trace lands on the cells themselves)."""
+    WRAP rolls it too (the back-trace lands on the cells themselves), under
+    CLAMP adds half the back-trace's miss on the edge cells."""
     shape = (5, 6, 7)
     rho = RNG.uniform(0, 1, shape + (1,))
     u = faces(shape, **{comp: float(shift)})
@@ -75,6 +76,11 @@ def test_integer_velocity_shifts_by_whole_cells(axis, comp, shift):
     src = np.clip(np.arange(n) - shift, 0, n - 1)
     clamped = np.take(rho, src, axis=axis)
     assert np.array_equal(oadvect.density_maccormack(rho, *u, order=1, clamp="NONE", boundary="CLAMP"), clamped)
+    # MacCormack under CLAMP: the back-trace of the shifted grid, clamped at the
+    # edge, leaves the correction 0.5 * (rho - back) on the cells it cannot return to
+    back = np.take(clamped, np.clip(np.arange(n) + shift, 0, n - 1), axis=axis)
+    assert np.array_equal(oadvect.density_maccormack(rho, *u, order=2, clamp="NONE", boundary="CLAMP"),
+                          clamped + 0.5 * (rho - back))
 
 
 @pytest.mark.parametrize("shift", [1, 2, 3])
