@@ -57,6 +57,19 @@ def test_zero_velocity_is_identity(order, bm, clamp):
     assert np.array_equal(out, rho)
 
 
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("bm", ["CLAMP", "WRAP", "BORDER"])
+def test_zero_velocity_negative_clamp_cuts_below_zero(order, bm):
+    """The NEGATIVE clamp (tf.maximum(d, 0) after the warp, data_structures.py:
+    1715-1735) on a density with negative cells and zero velocity: max(rho, 0);
+    without a clamp the density itself."""
+    rho = RNG.uniform(-1, 1, (5, 6, 7, 1))
+    u = faces((5, 6, 7))
+    out = oadvect.density_maccormack(rho, *u, order=order, clamp="NEGATIVE", boundary=bm)
+    assert np.array_equal(out, np.maximum(rho, 0.0)) and np.any(rho < 0)
+    assert np.array_equal(oadvect.density_maccormack(rho, *u, order=order, clamp="NONE", boundary=bm), rho)
+
+
 @pytest.mark.parametrize("axis,comp", [(2, "ux"), (1, "uy"), (0, "uz")])
 @pytest.mark.parametrize("shift", [1, 2, -1])
 def test_integer_velocity_shifts_by_whole_cells(axis, comp, shift):
